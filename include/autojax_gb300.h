@@ -1,0 +1,238 @@
+/*
+ * autojax_gb300 — C ABI of the GB300 (sm_103a) interferometer inversion kernels.
+ *
+ * Conventions shared by every entry point:
+ *   - pointers are DEVICE pointers to C-contiguous (row-major) arrays with the
+ *     reference's dtypes: double for float64, int64_t for int64, interleaved
+ *     (re, im) doubles for complex128, uint8_t (0/1) for bool;
+ *   - the caller owns every buffer; nothing here allocates device memory.
+ *     Scratch comes from a caller-provided workspace whose size the matching
+ *     *_workspace_size() function returns;
+ *   - work is enqueued on `stream` (a cudaStream_t, NULL = legacy default) and
+ *     nothing synchronises, so calls can be captured in CUDA graphs;
+ *   - the return value reports argument and launch errors (AJ_OK or a
+ *     negative AJ_ERR_*). Data-dependent failures found on the device (an
+ *     out-of-range index, a non-positive-definite pivot) are written to the
+ *     caller's device word `info` (0 = fine; see AJ_INFO_*), like cuSOLVER's
+ *     devInfo; the caller reads it after the stream work completes;
+ *   - `precision` selects AJ_FP64 (IEEE float64 throughout, the parity path)
+ *     or AJ_MIXED (FP64 phase reduction and factorisations, FP32 cos sums with
+ *     compensated accumulation and FP32 contractions).
+ *
+ * Each declaration names the function of ickc/python-autojax it replaces
+ * (file:line in src/autojax/).
+ */
+#ifndef AUTOJAX_GB300_H
+#define AUTOJAX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AJ_OK 0
+#define AJ_ERR_ARG (-1)       /* bad size, null pointer, unknown precision */
+#define AJ_ERR_CUDA (-2)      /* a launch failed; see aj_last_cuda_error() */
+#define AJ_ERR_WORKSPACE (-3) /* workspace smaller than *_workspace_size() */
+
+#define AJ_INFO_OK 0
+#define AJ_INFO_INDEX_RANGE 1       /* an index was outside [0, n) and not -1 */
+#define AJ_INFO_NOT_POSITIVE_DEFINITE 2 /* Cholesky met a pivot <= 0 or NaN */
+
+#define AJ_FP64 0
+#define AJ_MIXED 1
+
+/* Library version string and the last CUDA error code seen by a launch. */
+const char* aj_version(void);
+int aj_last_cuda_error(void);
+/* Kernel launches this library has issued in the process (for launch accounting). */
+unsigned long long aj_launch_count(void);
+/* Arithmetic-throughput probe: `blocks` x 256 threads, each running 8 independent
+ * fused multiply-add chains for iters x 16 steps (fp32 or fp64); `out` holds
+ * blocks * 256 elements of that type. flops = 2 * 128 * iters * blocks * 256. */
+int aj_probe_fma(int precision, int64_t blocks, int iters, void* out, void* stream);
+/* Number of info words a caller should provide (the first holds the code,
+ * the second the failing index or pivot). */
+#define AJ_INFO_WORDS 2
+
+/* ---------------------------------------------------------------- geometry */
+
+/* numba.py:50-86 mask_2d_circular_from (centre via numba.py:13-44).
+ * mask[ny][nx] = radius^2 < ((y - cy) psy)^2 + ((x - cx) psx)^2, bit-exact. */
+int aj_mask_2d_circular(int64_t ny, int64_t nx, double psy, double psx, double radius, double centre_y,
+                        double centre_x, uint8_t* mask, void* stream);
+
+/* tests.py:279-281, 304-306 (native_index_for_slim_index = argwhere(~mask),
+ * grid_radians_slim = grid_2d[~mask]). Writes the unmasked count to *count
+ * (device int64) and, row-major, up to max_out (row, col) pairs; grid_2d
+ * (ny, nx, 2) and grid_slim (max_out, 2) may be NULL. */
+int aj_slim_from_mask(const uint8_t* mask, int64_t ny, int64_t nx, const double* grid_2d, int64_t max_out,
+                      int64_t* native_index, double* grid_slim, int64_t* count, void* stream);
+
+/* ------------------------------------------------------- w_tilde family */
+
+/* numba.py:156-207 w_tilde_curvature_interferometer_from.
+ * W[i][j] = sum_k noise_k^-2 cos(2 pi ((x_i - x_j) u_k + (y_i - y_j) v_k)),
+ * x = grid[:,1] with u = uv[:,0], y = grid[:,0] with v = uv[:,1].
+ * Computed as the K-deep symmetric product C C^T + S S^T of the
+ * sqrt(w)-scaled cos/sin panels (exact identity cos(a-b) = cos a cos b +
+ * sin a sin b). out64 (M, M) is always written; out32 (M, M, may be NULL)
+ * receives a float copy for the mixed pipeline. */
+size_t aj_w_tilde_curvature_workspace_size(int64_t K, int64_t M, int precision);
+int aj_w_tilde_curvature(const double* noise_map_real, const double* uv, const double* grid_slim, int64_t K,
+                         int64_t M, double* out64, float* out32, void* workspace, size_t workspace_bytes,
+                         int precision, void* stream);
+
+/* numba.py:211-234 w_compact_curvature_interferometer_from.
+ * out (N, 2N-1): w_c[n0][n1+N-1] = sum_k noise_k^-2 cos(D (n1 u_k - n0 v_k)),
+ * D = pi^2 pixel_scale / 324000. */
+size_t aj_w_compact_curvature_workspace_size(int64_t N, int64_t K, int precision);
+int aj_w_compact_curvature(int64_t N, const double* noise_map_real, const double* uv, int64_t K,
+                           double pixel_scale, double* out, void* workspace, size_t workspace_bytes,
+                           int precision, void* stream);
+
+/* original.py:230-403 w_tilde_curvature_preload_interferometer_from.
+ * out (2Y, 2X): the four corner-offset quadrants of the (Y, X) block of
+ * grid_2d (gy, gx, 2), gy >= Y, gx >= X. Row Y and column X stay zero. */
+size_t aj_w_tilde_preload_workspace_size(int64_t Y, int64_t X, int64_t K, int precision);
+int aj_w_tilde_preload(const double* noise_map_real, const double* uv, int64_t K, int64_t Y, int64_t X,
+                       const double* grid_2d, int64_t gy, int64_t gx, double* out, void* workspace,
+                       size_t workspace_bytes, int precision, void* stream);
+
+/* numba.py:95-152 w_tilde_data_interferometer_from.
+ * out[i] = sum_k (noise_k^2 / vis_k)^2 cos(2 pi (g_i1 u_k + g_i0 v_k)). */
+size_t aj_w_tilde_data_workspace_size(int64_t M, int64_t K, int precision);
+int aj_w_tilde_data(const double* visibilities_real, const double* noise_map_real, const double* uv,
+                    const double* grid_slim, int64_t K, int64_t M, double* out, void* workspace,
+                    size_t workspace_bytes, int precision, void* stream);
+
+/* numba.py:238-255 w_tilde_via_compact_from. out64/out32 (M, M), either may be NULL.
+ * Offsets outside the table set info = AJ_INFO_INDEX_RANGE and write 0. */
+int aj_w_tilde_via_compact(const double* w_compact, int64_t N, const int64_t* native_index, int64_t M,
+                           double* out64, float* out32, int* info, void* stream);
+
+/* numba.py:259-290 w_tilde_via_preload_from: W[i][j] = preload[y_j - y_i][x_j - x_i]
+ * with negative indices wrapping once, as NumPy indexing does. */
+int aj_w_tilde_via_preload(const double* preload, int64_t py, int64_t px, const int64_t* native_index, int64_t M,
+                           double* out64, float* out32, int* info, void* stream);
+
+/* ------------------------------------------------------ mapping matrix */
+
+/* numba.py:294-376 mapping_matrix_from: out (M, S) dense; rows stop at the
+ * first -1; a repeated index keeps the last weight. */
+int aj_mapping_matrix(const int64_t* pix_indexes, const double* pix_weights, int64_t M, int64_t B, int64_t S,
+                      double* out, int* info, void* stream);
+
+/* numba.py:380-406 data_vector_from: out (S,) = dirty_image (M,) @ mapping (M, S). */
+int aj_data_vector(const double* mapping_matrix, const double* dirty_image, int64_t M, int64_t S, double* out,
+                   void* stream);
+
+/* numba.py:410-435 curvature_matrix_via_w_tilde_from: out (S, S) = T^T W T
+ * (dense T (M, S), dense W (M, M)); workspace holds W T. */
+size_t aj_curvature_dense_workspace_size(int64_t M, int64_t S);
+int aj_curvature_dense(const double* w_tilde, const double* mapping_matrix, int64_t M, int64_t S, double* out,
+                       void* workspace, size_t workspace_bytes, void* stream);
+
+/* Sparse (index, weight) mapping products. The workspace holds the
+ * column-compressed transpose of T built on the device. */
+size_t aj_sparse_workspace_size(int64_t M, int64_t B, int64_t S, int64_t cols);
+
+/* numba.py:553-587 sparse_mapping_matrix_transpose_matmul: out (S, cols) = T^T matrix (M, cols). */
+int aj_sparse_mapping_matrix_transpose_matmul(const double* matrix, int64_t M, int64_t cols,
+                                              const int64_t* pix_indexes, const double* pix_weights, int64_t B,
+                                              int64_t S, double* out, void* workspace, size_t workspace_bytes,
+                                              int* info, void* stream);
+
+/* numba.py:591-614 curvature_matrix_via_w_wilde_sparse_mapping_matrix_from:
+ * out (S, S) = T^T (T^T W)^T. */
+int aj_curvature_w_tilde_sparse(const double* w_tilde, int64_t M, const int64_t* pix_indexes,
+                                const double* pix_weights, int64_t B, int64_t S, double* out, void* workspace,
+                                size_t workspace_bytes, int* info, void* stream);
+
+/* numba.py:500-549 _w_compact_matmul_sparse_mapping_matrix_from: out (M, S) = W T
+ * with W gathered from the compact table (N, 2N-1) on the fly. */
+int aj_w_compact_matmul_sparse(const double* w_compact, int64_t N, const int64_t* native_index, int64_t M,
+                               const int64_t* pix_indexes, const double* pix_weights, int64_t B, int64_t S,
+                               double* out, void* workspace, size_t workspace_bytes, int* info, void* stream);
+
+/* numba.py:618-647 curvature_matrix_via_w_compact_sparse_mapping_matrix_from
+ * (= numba.py:651-653 curvature_matrix_via_w_tilde_curvature_preload_interferometer_from,
+ *  and the result of numba.py:439-496 ..._direct_from): out (S, S). */
+int aj_curvature_w_compact_sparse(const double* w_compact, int64_t N, const int64_t* native_index, int64_t M,
+                                  const int64_t* pix_indexes, const double* pix_weights, int64_t B, int64_t S,
+                                  double* out, void* workspace, size_t workspace_bytes, int* info, void* stream);
+
+/* original.py:600-700 curvature_matrix_via_w_tilde_curvature_preload_interferometer_from:
+ * F from the (2Y, 2X) preload table with original.py's pix_size rows. */
+size_t aj_curvature_preload_original_workspace_size(int64_t M, int64_t B, int64_t S);
+int aj_curvature_preload_original(const double* preload, int64_t py, int64_t px, const int64_t* pix_indexes,
+                                  const int64_t* pix_sizes, const double* pix_weights, int64_t B,
+                                  const int64_t* native_index, int64_t M, int64_t S, double* out,
+                                  void* workspace, size_t workspace_bytes, int* info, void* stream);
+
+/* original.py:453-545 mapping_matrix_from (accumulating, sub-gridded form). */
+int aj_mapping_matrix_original(const int64_t* pix_indexes, const int64_t* pix_sizes, const double* pix_weights,
+                               int64_t n_sub, int64_t B, int64_t S, int64_t M, const int64_t* slim_index,
+                               const double* sub_fraction, double* out, int* info, void* stream);
+
+/* -------------------------------------------------- regularisation, solve */
+
+/* numba.py:657-695 constant_regularization_matrix_from: out (S, S). */
+int aj_constant_regularization(double coefficient, const int64_t* neighbors, const int64_t* neighbors_sizes,
+                               int64_t S, int64_t P, double* out, int* info, void* stream);
+
+/* numba.py:699-731 reconstruction_positive_negative_from: out (S,) = A^-1 D by
+ * a blocked FP64 Cholesky (A symmetric positive definite; the reference's LU
+ * also accepts indefinite A — here such A sets AJ_INFO_NOT_POSITIVE_DEFINITE). */
+size_t aj_spd_solve_workspace_size(int64_t S);
+int aj_spd_solve(const double* data_vector, const double* A, int64_t S, double* out, void* workspace,
+                 size_t workspace_bytes, int* info, void* stream);
+
+/* log|det A| of a symmetric positive definite A (the slogdet of numba.py:849-850). */
+int aj_spd_logdet(const double* A, int64_t S, double* out, void* workspace, size_t workspace_bytes, int* info,
+                  void* stream);
+
+/* numba.py:735-752 noise_normalization_complex_from: *out = 2 (K log 2pi + sum log|Re| + sum log|Im|). */
+int aj_noise_normalization(const double* noise_map_c128, int64_t K, double* out, void* stream);
+
+/* ------------------------------------------------------------ likelihood */
+
+/* Dimensions and inputs of one log-evidence evaluation. The shared W (M, M)
+ * is w_tilde64 (AJ_FP64) or w_tilde32 (AJ_MIXED); for the compact variant
+ * w_compact (N, 2N-1) and native_index (M, 2) replace it. */
+typedef struct aj_problem {
+    int64_t M, K, S, B, P, N;
+    const double* dirty_image;       /* (M,) */
+    const double* data;              /* (K,) complex128 */
+    const double* noise_map;         /* (K,) complex128 */
+    const double* w_tilde64;         /* (M, M) or NULL */
+    const float* w_tilde32;          /* (M, M) or NULL */
+    const double* w_compact;         /* (N, 2N-1) or NULL */
+    const int64_t* native_index;     /* (M, 2) or NULL */
+    const int64_t* pix_indexes;      /* (M, B) */
+    const double* pix_weights;       /* (M, B) */
+    const int64_t* neighbors;        /* (S, P) */
+    const int64_t* neighbors_sizes;  /* (S,) */
+    double coefficient;              /* regularisation coefficient c, lambda = c^2 */
+    const double* coefficient_dev;   /* optional device copy of c (read instead of `coefficient` when set,
+                                        so a captured CUDA graph can be replayed with new values) */
+} aj_problem;
+
+/* Outputs (device): out[0] = logE; with gradients out[1] = dlogE/dlambda and
+ * grad_weights (M, B) = dlogE/dpix_weights (zero where a weight does not
+ * reach the mapping matrix). reconstruction (S,) may be NULL. */
+size_t aj_log_evidence_workspace_size(const aj_problem* p, int precision, int with_grad);
+
+/* numba.py:761-857 log_likelihood_function_via_w_tilde_from (w_tilde set) and
+ * numba.py:866-967 log_likelihood_function_via_w_compact_from (w_compact set);
+ * `coefficient` generalises the reference's hard-coded 1.0 (numba.py:819). */
+int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* out, double* grad_weights,
+                    double* reconstruction, void* workspace, size_t workspace_bytes, int* info, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AUTOJAX_GB300_H */

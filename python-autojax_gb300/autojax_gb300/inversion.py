@@ -1,0 +1,235 @@
+"""Repeated log-evidence evaluations against one resident dataset (the MCMC inner loop).
+
+``LogEvidence`` keeps the dataset (dirty image, visibilities, noise, and the
+shared w_tilde or compact table) on the device, owns persistent input buffers
+and one workspace, and evaluates logE (and its adjoint) with a single C-ABI
+call per evaluation.  ``capture()`` records that call into a CUDA graph so a
+step replays ~300 kernel launches as one graph launch; the regularisation
+coefficient lives in device memory, so replays may change it.
+
+``LogEvidenceFunction`` exposes the same evaluation to ``torch.autograd`` with
+gradients for the mapping weights and the regularisation coefficient.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._device import PRECISIONS, precision_code
+
+
+def _as_dev(x, dtype, device):
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=dtype).contiguous()
+    return torch.as_tensor(np.ascontiguousarray(x), dtype=dtype).to(device)
+
+
+def _complex_real(x, device):
+    if isinstance(x, torch.Tensor):
+        return torch.view_as_real(x.to(device=device, dtype=torch.complex128).contiguous()).contiguous()
+    a = np.ascontiguousarray(x, dtype=np.complex128)
+    return torch.from_numpy(a.view(np.float64).reshape(-1, 2)).to(device)
+
+
+class LogEvidence:
+    """Resident-dataset evaluator of the log-evidence and its gradient.
+
+    Parameters mirror ``log_likelihood_function_via_w_tilde_from``
+    (numba.py:761-857): pass ``w_tilde`` (M, M), or ``w_compact`` (N, 2N-1)
+    with ``native_index_for_slim_index`` for the compact form (numba.py:866-967).
+    Shapes of the per-model arrays (M x B mapping, S x P neighbours) are fixed
+    at construction by ``B``, ``S`` and ``P``.
+    """
+
+    def __init__(self, dirty_image, data, noise_map, w_tilde=None, *, w_compact=None, native_index_for_slim_index=None,
+                 S: int, B: int, P: int, precision: str = "mixed", with_grad: bool = True, device=None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("LogEvidence needs a CUDA device (autojax_gb300 has no CPU path)")
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        dev = self.device
+        self.lib = _lib.load()
+        self.precision = precision
+        self.pc = precision_code(precision)
+        self.with_grad = bool(with_grad)
+        self.dirty = _as_dev(dirty_image, torch.float64, dev)
+        self.data = _complex_real(data, dev)
+        self.noise = _complex_real(noise_map, dev)
+        self.M = self.dirty.shape[0]
+        self.K = self.data.shape[0]
+        self.S, self.B, self.P = int(S), int(B), int(P)
+        self.w_tilde = _as_dev(w_tilde, torch.float64, dev) if w_tilde is not None else None
+        self.w_compact = _as_dev(w_compact, torch.float64, dev) if w_compact is not None else None
+        self.native = (_as_dev(native_index_for_slim_index, torch.int64, dev)
+                       if native_index_for_slim_index is not None else None)
+        if self.w_tilde is None and (self.w_compact is None or self.native is None):
+            raise ValueError("pass w_tilde, or w_compact with native_index_for_slim_index")
+        # persistent per-model inputs (graph replays read these addresses)
+        self.pix_indexes = torch.zeros((self.M, self.B), dtype=torch.int64, device=dev)
+        self.pix_weights = torch.zeros((self.M, self.B), dtype=torch.float64, device=dev)
+        self.neighbors = torch.full((self.S, self.P), -1, dtype=torch.int64, device=dev)
+        self.neighbors_sizes = torch.zeros(self.S, dtype=torch.int64, device=dev)
+        self.coefficient = torch.ones(1, dtype=torch.float64, device=dev)
+        # outputs
+        self.out = torch.zeros(2, dtype=torch.float64, device=dev)
+        self.grad_weights = torch.zeros((self.M, self.B), dtype=torch.float64, device=dev)
+        self.reconstruction = torch.zeros(self.S, dtype=torch.float64, device=dev)
+        self.info = torch.zeros(2, dtype=torch.int32, device=dev)
+        self.problem = self._problem()
+        nbytes = self.lib.aj_log_evidence_workspace_size(self.problem, self.pc, int(self.with_grad))
+        if nbytes == 0:
+            raise ValueError("inconsistent problem dimensions")
+        self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        self.graph = None
+        self.launches_per_eval = None
+        # pinned staging for host inputs/outputs (end-to-end calls)
+        self._h_idx = torch.empty((self.M, self.B), dtype=torch.int64).pin_memory()
+        self._h_w = torch.empty((self.M, self.B), dtype=torch.float64).pin_memory()
+        self._h_nb = torch.empty((self.S, self.P), dtype=torch.int64).pin_memory()
+        self._h_nsz = torch.empty(self.S, dtype=torch.int64).pin_memory()
+        self._h_coef = torch.empty(1, dtype=torch.float64).pin_memory()
+        self._h_out = torch.empty(2, dtype=torch.float64).pin_memory()
+        self._h_grad = torch.empty((self.M, self.B), dtype=torch.float64).pin_memory()
+
+    def _problem(self) -> _lib.Problem:
+        p = _lib.Problem()
+        p.M, p.K, p.S, p.B, p.P = self.M, self.K, self.S, self.B, self.P
+        p.dirty_image = self.dirty.data_ptr()
+        p.data = self.data.data_ptr()
+        p.noise_map = self.noise.data_ptr()
+        if self.w_tilde is not None:
+            p.w_tilde64 = self.w_tilde.data_ptr()
+        else:
+            p.w_compact = self.w_compact.data_ptr()
+            p.native_index = self.native.data_ptr()
+            p.N = self.w_compact.shape[0]
+        p.pix_indexes = self.pix_indexes.data_ptr()
+        p.pix_weights = self.pix_weights.data_ptr()
+        p.neighbors = self.neighbors.data_ptr()
+        p.neighbors_sizes = self.neighbors_sizes.data_ptr()
+        p.coefficient = 1.0
+        p.coefficient_dev = self.coefficient.data_ptr()
+        return p
+
+    # ---------------------------------------------------------------- inputs
+
+    def set_model(self, pix_indexes, pix_weights, neighbors, neighbors_sizes, coefficient=1.0):
+        """Copy one lens model's arrays into the persistent device buffers (device-to-device for tensors)."""
+        self.pix_indexes.copy_(_as_dev(pix_indexes, torch.int64, self.device))
+        self.pix_weights.copy_(_as_dev(pix_weights, torch.float64, self.device))
+        nb = _as_dev(neighbors, torch.int64, self.device)
+        self.neighbors.fill_(-1)
+        self.neighbors[:, : nb.shape[1]].copy_(nb)
+        self.neighbors_sizes.copy_(_as_dev(neighbors_sizes, torch.int64, self.device))
+        self.set_coefficient(coefficient)
+
+    def set_coefficient(self, coefficient):
+        if isinstance(coefficient, torch.Tensor):
+            self.coefficient.copy_(coefficient.reshape(1).to(self.coefficient))
+        else:
+            self.coefficient.fill_(float(coefficient))
+
+    # ------------------------------------------------------------- execution
+
+    def launch(self):
+        """Enqueue one evaluation on the current stream (no synchronisation)."""
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        self.info.zero_()
+        rc = self.lib.aj_log_evidence(self.problem, self.pc, int(self.with_grad), self.out.data_ptr(),
+                                      self.grad_weights.data_ptr() if self.with_grad else None,
+                                      self.reconstruction.data_ptr(), self.workspace.data_ptr(),
+                                      self.workspace.numel(), self.info.data_ptr(), stream)
+        _lib.check(rc, "aj_log_evidence")
+
+    def capture(self):
+        """Record one evaluation into a CUDA graph (after a warm-up call); step() then replays it."""
+        self.launch()
+        torch.cuda.synchronize(self.device)
+        before = self.lib.aj_launch_count()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.launch()
+        self.launches_per_eval = int(self.lib.aj_launch_count() - before)
+        self.graph = g
+        return g
+
+    def step(self):
+        """One evaluation: graph replay when captured, else a direct launch."""
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self.launch()
+
+    def check(self):
+        code, where = (int(v) for v in self.info.tolist())
+        if code == _lib.AJ_INFO_NOT_POSITIVE_DEFINITE:
+            raise np.linalg.LinAlgError(f"curvature_reg_matrix is not positive definite (pivot {where})")
+        if code == _lib.AJ_INFO_INDEX_RANGE:
+            raise IndexError(f"index out of range (flat position {where})")
+
+    # --------------------------------------------------------- host facing
+
+    def evaluate_host(self, pix_indexes, pix_weights, neighbors, neighbors_sizes, coefficient=1.0):
+        """End-to-end call with host NumPy inputs: H2D from pinned memory, one evaluation, D2H of the results.
+
+        Returns (logE, dlogE/dlambda, dlogE/dpix_weights) as NumPy values.
+        """
+        self._h_idx.numpy()[...] = pix_indexes
+        self._h_w.numpy()[...] = pix_weights
+        nb = np.asarray(neighbors)
+        self._h_nb.numpy()[...] = -1
+        self._h_nb.numpy()[:, : nb.shape[1]] = nb
+        self._h_nsz.numpy()[...] = neighbors_sizes
+        self._h_coef.numpy()[0] = coefficient
+        self.pix_indexes.copy_(self._h_idx, non_blocking=True)
+        self.pix_weights.copy_(self._h_w, non_blocking=True)
+        self.neighbors.copy_(self._h_nb, non_blocking=True)
+        self.neighbors_sizes.copy_(self._h_nsz, non_blocking=True)
+        self.coefficient.copy_(self._h_coef, non_blocking=True)
+        self.step()
+        self._h_out.copy_(self.out, non_blocking=True)
+        if self.with_grad:
+            self._h_grad.copy_(self.grad_weights, non_blocking=True)
+        torch.cuda.current_stream(self.device).synchronize()
+        self.check()
+        o = self._h_out.numpy()
+        return float(o[0]), float(o[1]), (self._h_grad.numpy().copy() if self.with_grad else None)
+
+    def h2d_bytes(self) -> int:
+        return sum(t.numel() * t.element_size() for t in (self._h_idx, self._h_w, self._h_nb, self._h_nsz, self._h_coef))
+
+    def d2h_bytes(self) -> int:
+        return self._h_out.numel() * 8 + (self._h_grad.numel() * 8 if self.with_grad else 0)
+
+
+class LogEvidenceFunction(torch.autograd.Function):
+    """logE(pix_weights, coefficient) for a LogEvidence evaluator with its model indices set.
+
+    Backward returns dlogE/dpix_weights and dlogE/dcoefficient = 2 c dlogE/dlambda.
+    """
+
+    @staticmethod
+    def forward(ctx, pix_weights: torch.Tensor, coefficient: torch.Tensor, evaluator: LogEvidence):
+        ev = evaluator
+        ev.pix_weights.copy_(pix_weights.detach())
+        ev.set_coefficient(coefficient.detach())
+        ev.step()
+        ev.check()
+        ctx.save_for_backward(coefficient.detach().clone().reshape(()))
+        ctx.grads = (ev.grad_weights.clone(), ev.out[1].clone())
+        return ev.out[0].clone()
+
+    @staticmethod
+    def backward(ctx, g):
+        (c,) = ctx.saved_tensors
+        gw, dlam = ctx.grads
+        return g * gw, (g * dlam * 2.0 * c).reshape(()), None
+
+
+def log_evidence(pix_weights: torch.Tensor, coefficient: torch.Tensor, evaluator: LogEvidence) -> torch.Tensor:
+    """Differentiable logE (see LogEvidenceFunction)."""
+    return LogEvidenceFunction.apply(pix_weights, coefficient, evaluator)
+
+
+__all__ = ["LogEvidence", "LogEvidenceFunction", "log_evidence", "PRECISIONS"]

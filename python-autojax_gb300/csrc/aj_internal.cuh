@@ -1,0 +1,69 @@
+// Host-side building blocks shared between the translation units.
+#pragma once
+
+#include "aj_common.cuh"
+
+namespace aj {
+
+// ---- linalg.cu
+
+// C (m x n) = alpha op(A) op(B) + beta C, row-major float64.
+// lower_only: only tiles on or below the diagonal of C are touched (square C).
+int gemm_f64(bool transA, bool transB, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+             const double* B, int64_t ldb, double beta, double* C, int64_t ldc, bool lower_only, cudaStream_t st);
+
+// out (cols x rows) = in (rows x cols)^T
+template <typename T>
+int transpose(const T* in, int64_t rows, int64_t cols, T* out, cudaStream_t st);
+
+// Cholesky-based SPD toolkit on a float64 S x S matrix (row-major, lower triangle used).
+struct SpdWorkspace {
+    double* L;        // S x S factor (lower), also holds scratch upper
+    double* Linv;     // S x S inverse factor (lower) or nullptr
+    double* dinv;     // nblocks x NB x NB inverses of the diagonal blocks
+    double* vec;      // S scratch
+    double* scal;     // 8 scratch scalars
+};
+size_t spd_workspace_bytes(int64_t S, bool with_inverse);
+SpdWorkspace spd_carve(Carver& cv, int64_t S, bool with_inverse);
+// L = chol(A) (A read, not modified); logdet written to *logdet (device); info on failure.
+int spd_factor(const double* A, int64_t S, SpdWorkspace& w, double* logdet, int* info, cudaStream_t st);
+// Linv = L^-1 (lower)
+int spd_invert_factor(int64_t S, SpdWorkspace& w, int* info, cudaStream_t st);
+// x = A^-1 b using L (triangular solves); b and x may alias
+int spd_solve_vec(int64_t S, SpdWorkspace& w, const double* b, double* x, int* info, cudaStream_t st);
+// Ainv (S x S, full symmetric) = Linv^T Linv
+int spd_inverse_from_factor(int64_t S, SpdWorkspace& w, double* Ainv, cudaStream_t st);
+
+// ---- mapping.cu
+
+// H = 1e-8 I + c^2 L (numba.py:686-694); c read from coefficient_dev when it is not null
+int regularization(double coefficient, const double* coefficient_dev, const int64_t* neighbors,
+                   const int64_t* neighbors_sizes, int64_t S, int64_t P, double* out, int* info, cudaStream_t st);
+
+// Column-compressed transpose of the sparse mapping (index, weight) rows.
+struct Csc {
+    int* colptr;   // S + 1
+    int* rows;     // nnz capacity M * B
+    double* vals;  // nnz capacity
+    int* keys;     // scratch, nnz capacity
+    int* cursor;   // S
+};
+enum CscMode { CSC_SUM = 0, CSC_ASSIGN = 1 };
+void csc_take(Carver& cv, int64_t M, int64_t B, int64_t S, Csc& c);
+size_t csc_bytes(int64_t M, int64_t B, int64_t S);
+// rows stop at the first -1 unless `sizes` is given (then row m uses its first sizes[m] entries)
+int csc_build(const int64_t* idx, const double* w, const int64_t* sizes, int64_t M, int64_t B, int64_t S, CscMode mode,
+              Csc& c, int* info, cudaStream_t st);
+// out (S x cols, ld_out) = T^T X (M x cols, ld_x) via the CSC; Tin/Tout float or double
+template <typename Tin, typename Tout>
+int csc_spmm_t(const Csc& c, int64_t S, const Tin* X, int64_t ld_x, int64_t cols, Tout* out, int64_t ld_out,
+               cudaStream_t st);
+// out[s] = sum_e val[e] * x[row[e]]
+int csc_spmv_t(const Csc& c, int64_t S, const double* x, double* out, cudaStream_t st);
+// TW (S x M) with TW[s][m1] = sum_e val[e] * Wc(m1, row[e]) from the compact table (T float or double)
+template <typename T>
+int csc_compact_tw(const Csc& c, int64_t S, const double* w_compact, int64_t N, const int64_t* native, int64_t M,
+                   T* TW, int* info, cudaStream_t st);
+
+}  // namespace aj

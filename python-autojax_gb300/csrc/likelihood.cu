@@ -1,0 +1,341 @@
+// The log-evidence of one lens-model evaluation and its adjoint
+// (numba.py:761-857, 866-967; the gradient has no reference counterpart).
+//
+//   logE = -1/2 [ chi.chi - s.D + log|A| - log|H| + norm ],  A = F + H,
+//   F = T^T W T,  D = T^T dirty,  s = A^-1 D,  H = 1e-8 I + lambda L.
+// With Omega = W T:
+//   dlogE/dlambda  = -1/2 [ s^T L s + tr(A^-1 L) - tr(H^-1 L) ],
+//                     tr(H^-1 L) = (S - 1e-8 tr(H^-1)) / lambda  (H^-1 L = (I - 1e-8 H^-1) / lambda),
+//   dlogE/dT[m, j] = dirty_m s_j - (Omega s)_m s_j - (Omega A^-1)[m, j],
+// read on the sparse pattern of the weights.  The w_tilde likelihood builds
+// both F and D from the dense mapping (a repeated index keeps its last
+// weight, numba.py:824-841); the compact one builds F from the summed sparse
+// rows and D from the dense mapping (numba.py:928-951) — both are kept.
+//
+// Dataset terms (chi.chi and sum log|noise|) are recomputed on every call;
+// sum log|x| is evaluated as log of frexp-normalised products of 32 values
+// plus the exponent sum, so the float64 pipe does one log per 32 inputs.
+
+#include <math.h>
+
+#include "aj_internal.cuh"
+
+namespace aj {
+
+constexpr int KT_THREADS = 256;
+constexpr int KT_PER_THREAD = 32;
+
+// partial[b] = (sum chi^2, sum log|noise|) over this block's chunk of the 2K reals
+__global__ void __launch_bounds__(KT_THREADS)
+    k_terms_kernel(const double* __restrict__ data, const double* __restrict__ noise, int64_t n2,
+                   double* __restrict__ partial) {
+    __shared__ double red[32];
+    const int64_t base = ((int64_t)blockIdx.x * KT_THREADS + threadIdx.x) * KT_PER_THREAD;
+    double chi2 = 0.0, mant = 1.0;
+    int64_t ex = 0;
+    for (int q = 0; q < KT_PER_THREAD; ++q) {
+        const int64_t t = base + q;
+        if (t < n2) {
+            const double x = noise[t];
+            const double r = data[t] / x;
+            chi2 = fma(r, r, chi2);
+            int e;
+            const double m = frexp(fabs(x), &e);
+            mant *= m;
+            ex += e;
+        }
+    }
+    double lg = log(mant) + (double)ex * 0.69314718055994530942;
+    chi2 = block_sum(chi2, red);
+    lg = block_sum(lg, red);
+    if (threadIdx.x == 0) {
+        partial[2 * blockIdx.x] = chi2;
+        partial[2 * blockIdx.x + 1] = lg;
+    }
+}
+
+// out[0] = logE from the partials, s.D, log|A|, log|H| (numba.py:846-857)
+__global__ void assemble_kernel(const double* __restrict__ partial, int64_t nblk, int64_t K,
+                                const double* __restrict__ s, const double* __restrict__ D, int64_t S,
+                                const double* __restrict__ logdets, double* __restrict__ out) {
+    __shared__ double red[32];
+    double chi2 = 0.0, lg = 0.0, sd = 0.0;
+    for (int64_t b = threadIdx.x; b < nblk; b += blockDim.x) {
+        chi2 += partial[2 * b];
+        lg += partial[2 * b + 1];
+    }
+    for (int64_t i = threadIdx.x; i < S; i += blockDim.x) sd = fma(s[i], D[i], sd);
+    chi2 = block_sum(chi2, red);
+    lg = block_sum(lg, red);
+    sd = block_sum(sd, red);
+    if (threadIdx.x == 0) {
+        const double norm = 2.0 * ((double)K * 1.8378770664093454836 + lg);  // log(2 pi)
+        out[0] = -0.5 * (chi2 - sd + logdets[0] - logdets[1] + norm);
+    }
+}
+
+__global__ void add_kernel(const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ c,
+                           int64_t n) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        c[t] = a[t] + b[t];
+}
+
+// partial sums of squares of a lower-triangular matrix (tr(H^-1) = ||L_H^-1||_F^2)
+__global__ void frob_lower_kernel(const double* __restrict__ Li, int64_t S, double* __restrict__ partial) {
+    __shared__ double red[32];
+    double acc = 0.0;
+    for (int64_t i = blockIdx.x; i < S; i += gridDim.x)
+        for (int64_t j = threadIdx.x; j <= i; j += blockDim.x) {
+            const double v = Li[i * S + j];
+            acc = fma(v, v, acc);
+        }
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+}
+
+// out[1] = dlogE/dlambda.  L's entries follow numba.py:688-694: diag(n), -1 per neighbour entry.
+__global__ void dlam_kernel(const int64_t* __restrict__ nb, const int64_t* __restrict__ nsz, int64_t S, int64_t P,
+                            const double* __restrict__ s, const double* __restrict__ Ainv,
+                            const double* __restrict__ frob_partial, int64_t nfrob, double coef,
+                            const double* __restrict__ coef_dev, double* __restrict__ out) {
+    const double c = coef_dev ? *coef_dev : coef;
+    const double lam = c * c;
+    __shared__ double red[32];
+    double sls = 0.0, tra = 0.0, trl = 0.0, trh = 0.0;
+    for (int64_t i = threadIdx.x; i < S; i += blockDim.x) {
+        const double ni = (double)nsz[i];
+        sls = fma(ni, s[i] * s[i], sls);
+        tra = fma(ni, Ainv[i * S + i], tra);
+        trl += ni;
+        for (int64_t j = 0; j < P; ++j) {
+            const int64_t k = nb[i * P + j];
+            if (k == -1) break;
+            if (k < 0 || k >= S) continue;
+            sls -= s[i] * s[k];
+            tra -= Ainv[k * S + i];
+            if (k == i) trl -= 1.0;
+        }
+    }
+    for (int64_t b = threadIdx.x; b < nfrob; b += blockDim.x) trh += frob_partial[b];
+    sls = block_sum(sls, red);
+    tra = block_sum(tra, red);
+    trl = block_sum(trl, red);
+    trh = block_sum(trh, red);
+    if (threadIdx.x == 0) {
+        // tr(H^-1 L): (S - eps tr(H^-1)) / lambda, or tr(L) / eps when lambda = 0 (H = eps I)
+        const double trHL = lam != 0.0 ? ((double)S - 1e-8 * trh) / lam : trl / 1e-8;
+        out[1] = -0.5 * (sls + tra - trHL);
+    }
+}
+
+// grad[m][b] for the weights; one warp per image pixel m
+__global__ void __launch_bounds__(256)
+    weight_grad_kernel(const int64_t* __restrict__ idx, int64_t M, int64_t B, int64_t S,
+                       const double* __restrict__ Om, const double* __restrict__ Ainv, const double* __restrict__ s,
+                       const double* __restrict__ dirty, int compact_mode, double* __restrict__ grad) {
+    const int lane = threadIdx.x & 31;
+    const int64_t m = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (m >= M) return;
+    const double* om = Om + m * S;
+    double oms = 0.0;
+    for (int64_t j = lane; j < S; j += 32) oms = fma(om[j], s[j], oms);
+    oms = warp_sum(oms);
+    const int64_t* row = idx + m * B;
+    bool ended = false;
+    for (int64_t b = 0; b < B; ++b) {
+        const int64_t sp = row[b];
+        if (sp == -1) ended = true;
+        double g = 0.0;
+        if (!ended && sp >= 0 && sp < S) {
+            bool last = true;  // not overwritten by a later entry (dense-mapping semantics)
+            for (int64_t q = b + 1; q < B; ++q) {
+                if (row[q] == -1) break;
+                if (row[q] == sp) last = false;
+            }
+            const bool keepD = last;
+            const bool keepF = compact_mode ? true : last;
+            double oa = 0.0;
+            if (keepF) {
+                const double* ar = Ainv + sp * S;
+                for (int64_t j = lane; j < S; j += 32) oa = fma(om[j], ar[j], oa);
+                oa = warp_sum(oa);
+            }
+            if (keepD) g += dirty[m] * s[sp];
+            if (keepF) g -= oms * s[sp] + oa;
+        }
+        if (lane == 0) grad[m * B + b] = g;
+    }
+}
+
+// single-block noise normalisation for the standalone drop-in call
+__global__ void noise_norm_kernel(const double* __restrict__ x, int64_t n2, int64_t K, double* __restrict__ out) {
+    __shared__ double red[32];
+    double lg = 0.0, mant = 1.0;
+    int64_t ex = 0;
+    int cnt = 0;
+    for (int64_t t = threadIdx.x; t < n2; t += blockDim.x) {
+        int e;
+        mant *= frexp(fabs(x[t]), &e);
+        ex += e;
+        if (++cnt == KT_PER_THREAD) {
+            lg += log(mant);
+            mant = 1.0;
+            cnt = 0;
+        }
+    }
+    lg += log(mant) + (double)ex * 0.69314718055994530942;
+    lg = block_sum(lg, red);
+    if (threadIdx.x == 0) *out = 2.0 * ((double)K * 1.8378770664093454836 + lg);
+}
+
+struct EvidenceBufs {
+    Csc ca{}, cs{};
+    SpdWorkspace wa{}, wh{};
+    double *TW, *Om, *F, *H, *A, *Ainv, *D, *s, *kpart, *fpart, *logdets;
+    int64_t nk_blocks, nfrob;
+    bool compact, grad;
+};
+
+// One routine both sizes (base == nullptr) and carves the workspace, so the two never disagree.
+size_t evidence_carve(const aj_problem* p, bool with_grad, void* base, size_t bytes, EvidenceBufs& b) {
+    const int64_t M = p->M, S = p->S, B = p->B;
+    b.compact = p->w_compact != nullptr;
+    b.grad = with_grad;
+    b.nk_blocks = (2 * p->K + (int64_t)KT_THREADS * KT_PER_THREAD - 1) / ((int64_t)KT_THREADS * KT_PER_THREAD);
+    if (b.nk_blocks < 1) b.nk_blocks = 1;
+    b.nfrob = 2 * (int64_t)num_sms();
+    Carver cv(base, base ? bytes : ~size_t(0) >> 1);
+    auto sub = [&](size_t n) {
+        char* at = cv.take<char>(n);
+        return Carver(at, n);
+    };
+    {
+        Carver c = sub(csc_bytes(M, B, S));
+        csc_take(c, M, B, S, b.ca);
+    }
+    if (b.compact) {
+        Carver c = sub(csc_bytes(M, B, S));
+        csc_take(c, M, B, S, b.cs);
+    } else {
+        b.cs = b.ca;
+    }
+    b.TW = cv.take<double>(S * M);
+    b.Om = cv.take<double>(M * S);
+    b.F = cv.take<double>(S * S);
+    b.H = cv.take<double>(S * S);
+    b.A = cv.take<double>(S * S);
+    {
+        Carver c = sub(spd_workspace_bytes(S, with_grad));
+        b.wa = spd_carve(c, S, with_grad);
+    }
+    {
+        Carver c = sub(spd_workspace_bytes(S, with_grad));
+        b.wh = spd_carve(c, S, with_grad);
+    }
+    b.Ainv = with_grad ? cv.take<double>(S * S) : nullptr;
+    b.D = cv.take<double>(S);
+    b.s = cv.take<double>(S);
+    b.kpart = cv.take<double>(2 * b.nk_blocks);
+    b.fpart = cv.take<double>(b.nfrob);
+    b.logdets = cv.take<double>(8);
+    return align_up(cv.used);
+}
+
+int check_problem(const aj_problem* p) {
+    if (!p) return AJ_ERR_ARG;
+    if (p->M < 0 || p->K < 0 || p->S <= 0 || p->B < 0 || p->P < 0) return AJ_ERR_ARG;
+    if (!p->dirty_image || !p->pix_indexes || !p->pix_weights || !p->neighbors_sizes) return AJ_ERR_ARG;
+    if (p->P > 0 && !p->neighbors) return AJ_ERR_ARG;
+    if (p->K > 0 && (!p->data || !p->noise_map)) return AJ_ERR_ARG;
+    if (p->w_compact) {
+        if (p->N <= 0 || !p->native_index) return AJ_ERR_ARG;
+    } else if (!p->w_tilde64) {
+        return AJ_ERR_ARG;
+    }
+    return AJ_OK;
+}
+
+}  // namespace aj
+
+using namespace aj;
+
+extern "C" {
+
+int aj_noise_normalization(const double* noise_map_c128, int64_t K, double* out, void* stream) {
+    if (K < 0 || !out || (K > 0 && !noise_map_c128)) return AJ_ERR_ARG;
+    noise_norm_kernel<<<1, 1024, 0, as_stream(stream)>>>(noise_map_c128, 2 * K, K, out);
+    return check_launch();
+}
+
+size_t aj_log_evidence_workspace_size(const aj_problem* p, int precision, int with_grad) {
+    (void)precision;
+    if (check_problem(p) != AJ_OK) return 0;
+    EvidenceBufs b;
+    return evidence_carve(p, with_grad != 0, nullptr, 0, b);
+}
+
+int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* out, double* grad_weights,
+                    double* reconstruction, void* workspace, size_t workspace_bytes, int* info, void* stream) {
+    AJ_TRY(check_problem(p));
+    if (precision != AJ_FP64 && precision != AJ_MIXED) return AJ_ERR_ARG;
+    if (!out || (with_grad && !grad_weights)) return AJ_ERR_ARG;
+    EvidenceBufs b;
+    const size_t need = evidence_carve(p, with_grad != 0, nullptr, 0, b);
+    if (!workspace || workspace_bytes < need) return AJ_ERR_WORKSPACE;
+    evidence_carve(p, with_grad != 0, workspace, workspace_bytes, b);
+    cudaStream_t st = as_stream(stream);
+    const int64_t M = p->M, S = p->S, B = p->B, K = p->K;
+
+    // sparse mapping: dense-mapping semantics for D (and for F of the w_tilde likelihood)
+    AJ_TRY(csc_build(p->pix_indexes, p->pix_weights, nullptr, M, B, S, CSC_ASSIGN, b.ca, info, st));
+    if (b.compact) AJ_TRY(csc_build(p->pix_indexes, p->pix_weights, nullptr, M, B, S, CSC_SUM, b.cs, info, st));
+    AJ_TRY(csc_spmv_t(b.ca, S, p->dirty_image, b.D, st));
+
+    // Omega = W T (via TW = T^T W, W symmetric), F = T^T Omega
+    if (b.compact)
+        AJ_TRY(csc_compact_tw<double>(b.cs, S, p->w_compact, p->N, p->native_index, M, b.TW, info, st));
+    else
+        AJ_TRY(csc_spmm_t<double, double>(b.cs, S, p->w_tilde64, M, M, b.TW, M, st));
+    AJ_TRY(transpose<double>(b.TW, S, M, b.Om, st));
+    AJ_TRY(csc_spmm_t<double, double>(b.cs, S, b.Om, S, S, b.F, S, st));
+
+    // H, A = F + H, factorisations and log-determinants
+    AJ_TRY(regularization(p->coefficient, p->coefficient_dev, p->neighbors, p->neighbors_sizes, S, p->P, b.H, info, st));
+    add_kernel<<<blocks_for(S * S, 256, 8 * num_sms()), 256, 0, st>>>(b.F, b.H, b.A, S * S);
+    AJ_LAUNCHED();
+    AJ_TRY(spd_factor(b.A, S, b.wa, b.logdets + 0, info, st));
+    AJ_TRY(spd_factor(b.H, S, b.wh, b.logdets + 1, info, st));
+    AJ_TRY(spd_solve_vec(S, b.wa, b.D, b.s, info, st));
+
+    // chi.chi and sum log|noise| over the 2K reals, then logE
+    if (K > 0) {
+        k_terms_kernel<<<(unsigned)b.nk_blocks, KT_THREADS, 0, st>>>(p->data, p->noise_map, 2 * K, b.kpart);
+        AJ_LAUNCHED();
+    } else if (cudaMemsetAsync(b.kpart, 0, sizeof(double) * 2 * b.nk_blocks, st) != cudaSuccess) {
+        return AJ_ERR_CUDA;
+    }
+    assemble_kernel<<<1, 1024, 0, st>>>(b.kpart, b.nk_blocks, K, b.s, b.D, S, b.logdets, out);
+    AJ_LAUNCHED();
+    if (reconstruction &&
+        cudaMemcpyAsync(reconstruction, b.s, sizeof(double) * S, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        return AJ_ERR_CUDA;
+    if (!with_grad) return AJ_OK;
+
+    // adjoint
+    AJ_TRY(spd_invert_factor(S, b.wa, info, st));
+    AJ_TRY(spd_inverse_from_factor(S, b.wa, b.Ainv, st));
+    AJ_TRY(spd_invert_factor(S, b.wh, info, st));
+    frob_lower_kernel<<<(unsigned)b.nfrob, 256, 0, st>>>(b.wh.Linv, S, b.fpart);
+    AJ_LAUNCHED();
+    dlam_kernel<<<1, 1024, 0, st>>>(p->neighbors, p->neighbors_sizes, S, p->P, b.s, b.Ainv, b.fpart, b.nfrob,
+                                    p->coefficient, p->coefficient_dev, out);
+    AJ_LAUNCHED();
+    if (M > 0 && B > 0) {
+        weight_grad_kernel<<<blocks_for(M * 32, 256), 256, 0, st>>>(p->pix_indexes, M, B, S, b.Om, b.Ainv, b.s,
+                                                                    p->dirty_image, b.compact ? 1 : 0, grad_weights);
+        AJ_LAUNCHED();
+    }
+    return AJ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,643 @@
+// Mapping matrix, sparse mapping products and the regularisation matrix
+// (numba.py:294-695, original.py:453-545, 600-700).
+//
+// The sparse (index, weight) rows of the mapping T (M x S, B entries a row)
+// are turned on the device into a column-compressed transpose: for every
+// source pixel s the list of (image pixel m, weight) that reference it,
+// sorted by (m, b) so every sum runs in the reference's loop order.  Products
+// with T^T then gather whole rows of the dense operand, coalesced, with no
+// atomics.  Two row semantics exist in the reference and both are kept:
+//   CSC_SUM    — every entry before the first -1 contributes (the sparse
+//                products, numba.py:580-586, 543-548);
+//   CSC_ASSIGN — a repeated index keeps only its last weight (the dense
+//                mapping_matrix_from, numba.py:369-375).
+
+#include "aj_internal.cuh"
+
+namespace aj {
+
+// ------------------------------------------------------------- dense T
+
+__global__ void mapping_dense_kernel(const int64_t* __restrict__ idx, const double* __restrict__ w, int64_t M,
+                                     int64_t B, int64_t S, double* __restrict__ out, int* info) {
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
+        for (int64_t b = 0; b < B; ++b) {
+            const int64_t s = idx[m * B + b];
+            if (s == -1) break;
+            if (s < 0 || s >= S) {
+                report(info, AJ_INFO_INDEX_RANGE, m * B + b);
+                continue;
+            }
+            out[m * S + s] = w[m * B + b];
+        }
+    }
+}
+
+// original.py:527-543: T[slim[i]][idx] += sub_fraction[slim[i]] * w over the first sizes[i] entries
+__global__ void mapping_original_kernel(const int64_t* __restrict__ idx, const int64_t* __restrict__ sizes,
+                                        const double* __restrict__ w, int64_t n_sub, int64_t B, int64_t S, int64_t M,
+                                        const int64_t* __restrict__ slim, const double* __restrict__ frac,
+                                        double* __restrict__ out, int* info) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_sub; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = slim[i];
+        if (r < 0 || r >= M) {
+            report(info, AJ_INFO_INDEX_RANGE, i);
+            continue;
+        }
+        const int64_t nb = sizes[i] < B ? sizes[i] : B;
+        for (int64_t b = 0; b < nb; ++b) {
+            const int64_t s = idx[i * B + b];
+            if (s < 0 || s >= S) {
+                report(info, AJ_INFO_INDEX_RANGE, i * B + b);
+                continue;
+            }
+            atomicAdd(&out[r * S + s], frac[r] * w[i * B + b]);
+        }
+    }
+}
+
+// D[s] = sum_m dirty[m] T[m][s]: 32 columns per block, 8 row groups, fixed-order reduction.
+__global__ void data_vector_dense_kernel(const double* __restrict__ T, const double* __restrict__ d, int64_t M,
+                                         int64_t S, double* __restrict__ out) {
+    __shared__ double part[8][32];
+    const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const int64_t s = blockIdx.x * 32 + lane;
+    double acc = 0.0;
+    if (s < S)
+        for (int64_t m = g; m < M; m += 8) acc = fma(d[m], T[m * S + s], acc);
+    part[g][lane] = acc;
+    __syncthreads();
+    if (g == 0 && s < S) {
+        double v = 0.0;
+        for (int q = 0; q < 8; ++q) v += part[q][lane];
+        out[s] = v;
+    }
+}
+
+// ------------------------------------------------------------------ CSC
+
+__device__ __forceinline__ bool csc_entry(const int64_t* idx, const int64_t* sizes, int64_t m, int64_t b, int64_t B,
+                                          int64_t S, CscMode mode, int64_t& s, int* info) {
+    const int64_t* row = idx + m * B;
+    if (sizes) {
+        const int64_t nb = sizes[m] < B ? sizes[m] : B;
+        if (b >= nb) return false;
+    } else {
+        for (int64_t q = 0; q <= b; ++q)
+            if (row[q] == -1) return false;
+    }
+    s = row[b];
+    if (s < 0 || s >= S) {
+        report(info, AJ_INFO_INDEX_RANGE, m * B + b);
+        return false;
+    }
+    if (mode == CSC_ASSIGN) {
+        const int64_t nb = sizes ? (sizes[m] < B ? sizes[m] : B) : B;
+        for (int64_t q = b + 1; q < nb; ++q) {
+            if (!sizes && row[q] == -1) break;
+            if (row[q] == s) return false;  // overwritten by a later entry
+        }
+    }
+    return true;
+}
+
+__global__ void csc_count_kernel(const int64_t* __restrict__ idx, const int64_t* __restrict__ sizes, int64_t M,
+                                 int64_t B, int64_t S, CscMode mode, int* __restrict__ count, int* info) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < M * B; e += (int64_t)gridDim.x * blockDim.x) {
+        int64_t s;
+        if (csc_entry(idx, sizes, e / B, e % B, B, S, mode, s, nullptr)) atomicAdd(&count[s], 1);
+    }
+}
+
+// single block exclusive scan of count[0..S) into colptr[0..S], cursor reset
+__global__ void csc_scan_kernel(int* __restrict__ count, int64_t S, int* __restrict__ colptr) {
+    __shared__ int warp_tot[32];
+    __shared__ int base;
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int64_t c0 = 0; c0 < S; c0 += blockDim.x) {
+        const int64_t t = c0 + threadIdx.x;
+        const int v = t < S ? count[t] : 0;
+        int x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[wid] = x;
+        __syncthreads();
+        int before = 0;
+        for (int w = 0; w < wid; ++w) before += warp_tot[w];
+        if (t < S) {
+            colptr[t] = base + before + x - v;
+            count[t] = 0;  // reused as the fill cursor
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int tot = 0;
+            for (int w = 0; w < nw; ++w) tot += warp_tot[w];
+            base += tot;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) colptr[S] = base;
+}
+
+__global__ void csc_fill_kernel(const int64_t* __restrict__ idx, const double* __restrict__ w,
+                                const int64_t* __restrict__ sizes, int64_t M, int64_t B, int64_t S, CscMode mode,
+                                const int* __restrict__ colptr, int* __restrict__ cursor, int* __restrict__ rows,
+                                double* __restrict__ vals, int* __restrict__ keys, int* info) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < M * B; e += (int64_t)gridDim.x * blockDim.x) {
+        int64_t s;
+        if (csc_entry(idx, sizes, e / B, e % B, B, S, mode, s, info)) {
+            const int pos = colptr[s] + atomicAdd(&cursor[s], 1);
+            rows[pos] = static_cast<int>(e / B);
+            vals[pos] = w[e];
+            keys[pos] = static_cast<int>(e);
+        }
+    }
+}
+
+// sort each column's entries by (m, b): the reference's loop order
+__global__ void csc_sort_kernel(const int* __restrict__ colptr, int64_t S, int* __restrict__ rows,
+                                double* __restrict__ vals, int* __restrict__ keys) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < S; s += (int64_t)gridDim.x * blockDim.x) {
+        const int b = colptr[s], e = colptr[s + 1];
+        for (int i = b + 1; i < e; ++i) {
+            const int k = keys[i], r = rows[i];
+            const double v = vals[i];
+            int j = i - 1;
+            while (j >= b && keys[j] > k) {
+                keys[j + 1] = keys[j];
+                rows[j + 1] = rows[j];
+                vals[j + 1] = vals[j];
+                --j;
+            }
+            keys[j + 1] = k;
+            rows[j + 1] = r;
+            vals[j + 1] = v;
+        }
+    }
+}
+
+// out[s][c] = sum_e val[e] X[row[e]][c]; grid (S, column blocks), V columns per thread
+template <typename Tin, typename Tout, int V>
+__global__ void __launch_bounds__(256)
+    csc_spmm_t_kernel(const int* __restrict__ colptr, const int* __restrict__ rows, const double* __restrict__ vals,
+                      const Tin* __restrict__ X, int64_t ld_x, int64_t cols, Tout* __restrict__ out, int64_t ld_out) {
+    using Acc = typename std::conditional<sizeof(Tin) == 8 || sizeof(Tout) == 8, double, float>::type;
+    const int64_t s = blockIdx.x;
+    const int64_t c0 = (blockIdx.y * (int64_t)blockDim.x + threadIdx.x) * V;
+    if (c0 >= cols) return;
+    const int b = colptr[s], e = colptr[s + 1];
+    Acc acc[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[v] = 0;
+    const bool full = c0 + V <= cols;
+    for (int q = b; q < e; ++q) {
+        const Tin* xr = X + (int64_t)rows[q] * ld_x + c0;
+        const Acc a = static_cast<Acc>(vals[q]);
+        if (full) {
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[v] = fma(a, static_cast<Acc>(__ldg(xr + v)), acc[v]);
+        } else {
+            for (int v = 0; v < V && c0 + v < cols; ++v) acc[v] = fma(a, static_cast<Acc>(__ldg(xr + v)), acc[v]);
+        }
+    }
+    Tout* o = out + s * ld_out + c0;
+    for (int v = 0; v < V && c0 + v < cols; ++v) o[v] = static_cast<Tout>(acc[v]);
+}
+
+// float4 fast path of the hot W T product: X rows 16-byte aligned, cols % 4 == 0
+__global__ void __launch_bounds__(256)
+    csc_spmm_t_f32x4_kernel(const int* __restrict__ colptr, const int* __restrict__ rows,
+                            const double* __restrict__ vals, const float* __restrict__ X, int64_t ld_x, int64_t cols,
+                            float* __restrict__ out, int64_t ld_out) {
+    const int64_t s = blockIdx.x;
+    const int64_t c0 = (blockIdx.y * (int64_t)blockDim.x + threadIdx.x) * 4;
+    if (c0 >= cols) return;
+    const int b = colptr[s], e = colptr[s + 1];
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int q = b; q < e; ++q) {
+        const float4 x = __ldg(reinterpret_cast<const float4*>(X + (int64_t)rows[q] * ld_x + c0));
+        const float a = static_cast<float>(vals[q]);
+        acc.x = fmaf(a, x.x, acc.x);
+        acc.y = fmaf(a, x.y, acc.y);
+        acc.z = fmaf(a, x.z, acc.z);
+        acc.w = fmaf(a, x.w, acc.w);
+    }
+    *reinterpret_cast<float4*>(out + s * ld_out + c0) = acc;
+}
+
+__global__ void csc_spmv_t_kernel(const int* __restrict__ colptr, const int* __restrict__ rows,
+                                  const double* __restrict__ vals, int64_t S, const double* __restrict__ x,
+                                  double* __restrict__ out) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < S; s += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int q = colptr[s]; q < colptr[s + 1]; ++q) acc = fma(vals[q], x[rows[q]], acc);
+        out[s] = acc;
+    }
+}
+
+// TW[s][m1] = sum_e val[e] Wc(m1, m2 = row[e]) with the compact lookup of numba.py:538-541.
+// Persistent over (s, 1024-column chunk) items so each block loads the table once.
+template <typename T, bool SMEM>
+__global__ void __launch_bounds__(256)
+    csc_compact_tw_kernel(const int* __restrict__ colptr, const int* __restrict__ rows,
+                          const double* __restrict__ vals, int64_t S, const double* __restrict__ wc, int64_t N,
+                          const int64_t* __restrict__ nat, int64_t M, T* __restrict__ TW, int* info) {
+    extern __shared__ unsigned char smem_raw[];
+    T* tab = reinterpret_cast<T*>(smem_raw);
+    const int64_t W = 2 * N - 1;
+    const T* tsrc;
+    if constexpr (SMEM) {
+        for (int64_t t = threadIdx.x; t < N * W; t += blockDim.x) tab[t] = static_cast<T>(wc[t]);
+        __syncthreads();
+        tsrc = tab;
+    }
+    const int64_t chunks = (M + 1023) / 1024;
+    const int64_t items = S * chunks;
+    for (int64_t it = blockIdx.x; it < items; it += gridDim.x) {
+        const int64_t s = it / chunks, ch = it - s * chunks;
+        int64_t r1[4], c1[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int64_t m1 = ch * 1024 + v * 256 + threadIdx.x;
+            r1[v] = m1 < M ? nat[2 * m1] : 0;
+            c1[v] = m1 < M ? nat[2 * m1 + 1] : 0;
+        }
+        T acc[4] = {0, 0, 0, 0};
+        for (int q = colptr[s]; q < colptr[s + 1]; ++q) {
+            const int64_t m2 = rows[q];
+            const int64_t r2 = nat[2 * m2], c2 = nat[2 * m2 + 1];
+            const T a = static_cast<T>(vals[q]);
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                const int64_t n1 = r1[v] - r2;
+                const int64_t n2 = (n1 >= 0 ? c1[v] - c2 : c2 - c1[v]) + (N - 1);
+                const int64_t ar = n1 < 0 ? -n1 : n1;
+                T wv = 0;
+                if (ar < N && n2 >= 0 && n2 < W) {
+                    if constexpr (SMEM)
+                        wv = tsrc[ar * W + n2];
+                    else
+                        wv = static_cast<T>(__ldg(wc + ar * W + n2));
+                } else if (ch * 1024 + v * 256 + threadIdx.x < M) {
+                    report(info, AJ_INFO_INDEX_RANGE, m2);
+                }
+                acc[v] = fma(a, wv, acc[v]);
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int64_t m1 = ch * 1024 + v * 256 + threadIdx.x;
+            if (m1 < M) TW[s * M + m1] = acc[v];
+        }
+    }
+}
+
+// symmetric expansion of original.py's preload pairs: W[i][j] = preload[yb - ya][xb - xa], (a, b) = (min, max)
+__global__ void expand_preload_sym_kernel(const double* __restrict__ pre, int64_t py, int64_t px,
+                                          const int64_t* __restrict__ nat, int64_t M, double* __restrict__ out,
+                                          int* info) {
+    for (int64_t i = blockIdx.y; i < M; i += gridDim.y) {
+        for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < M; j += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t a = i < j ? i : j, b = i < j ? j : i;
+            int64_t r = nat[2 * b] - nat[2 * a], c = nat[2 * b + 1] - nat[2 * a + 1];
+            if (r < 0) r += py;
+            if (c < 0) c += px;
+            double v = 0.0;
+            if (r >= 0 && r < py && c >= 0 && c < px)
+                v = pre[r * px + c];
+            else
+                report(info, AJ_INFO_INDEX_RANGE, i * M + j);
+            out[i * M + j] = v;
+        }
+    }
+}
+
+// -------------------------------------------------------- regularisation
+
+// numba.py:686-694: diag(1e-8 + c^2 n_i), then H[i][k] -= c^2 along the row until -1
+__global__ void regularization_kernel(double coef, const double* __restrict__ coef_dev, const int64_t* __restrict__ nb,
+                                      const int64_t* __restrict__ nsz, int64_t S, int64_t P, double* __restrict__ H,
+                                      int* info) {
+    const double c = coef_dev ? *coef_dev : coef;
+    const double c2 = c * c;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < S; i += (int64_t)gridDim.x * blockDim.x) {
+        H[i * S + i] = __dadd_rn(1e-8, __dmul_rn(c2, (double)nsz[i]));
+        for (int64_t j = 0; j < P; ++j) {
+            const int64_t k = nb[i * P + j];
+            if (k == -1) break;
+            if (k < 0 || k >= S) {
+                report(info, AJ_INFO_INDEX_RANGE, i * P + j);
+                continue;
+            }
+            H[i * S + k] = __dsub_rn(H[i * S + k], c2);
+        }
+    }
+}
+
+// ------------------------------------------------------------ host side
+
+int regularization(double coefficient, const double* coefficient_dev, const int64_t* neighbors,
+                   const int64_t* neighbors_sizes, int64_t S, int64_t P, double* out, int* info, cudaStream_t st) {
+    if (cudaMemsetAsync(out, 0, sizeof(double) * S * S, st) != cudaSuccess) return AJ_ERR_CUDA;
+    regularization_kernel<<<blocks_for(S, 128, 8 * num_sms()), 128, 0, st>>>(coefficient, coefficient_dev, neighbors,
+                                                                           neighbors_sizes, S, P, out, info);
+    return check_launch();
+}
+
+size_t csc_bytes(int64_t M, int64_t B, int64_t S) {
+    Sizer s;
+    s.take<int>(S + 1);
+    s.take<int>(M * B);
+    s.take<double>(M * B);
+    s.take<int>(M * B);
+    s.take<int>(S);
+    return s.total();
+}
+
+void csc_take(Carver& cv, int64_t M, int64_t B, int64_t S, Csc& c) {
+    c.colptr = cv.take<int>(S + 1);
+    c.rows = cv.take<int>(M * B);
+    c.vals = cv.take<double>(M * B);
+    c.keys = cv.take<int>(M * B);
+    c.cursor = cv.take<int>(S);
+}
+
+int csc_build(const int64_t* idx, const double* w, const int64_t* sizes, int64_t M, int64_t B, int64_t S, CscMode mode,
+              Csc& c, int* info, cudaStream_t st) {
+    if (cudaMemsetAsync(c.cursor, 0, sizeof(int) * S, st) != cudaSuccess) return AJ_ERR_CUDA;
+    const unsigned g = blocks_for(M * B, 256, 16 * num_sms());
+    csc_count_kernel<<<g, 256, 0, st>>>(idx, sizes, M, B, S, mode, c.cursor, info);
+    AJ_LAUNCHED();
+    csc_scan_kernel<<<1, 1024, 0, st>>>(c.cursor, S, c.colptr);
+    AJ_LAUNCHED();
+    csc_fill_kernel<<<g, 256, 0, st>>>(idx, w, sizes, M, B, S, mode, c.colptr, c.cursor, c.rows, c.vals, c.keys, info);
+    AJ_LAUNCHED();
+    csc_sort_kernel<<<blocks_for(S, 128, 8 * num_sms()), 128, 0, st>>>(c.colptr, S, c.rows, c.vals, c.keys);
+    return check_launch();
+}
+
+template <typename Tin, typename Tout>
+int csc_spmm_t(const Csc& c, int64_t S, const Tin* X, int64_t ld_x, int64_t cols, Tout* out, int64_t ld_out,
+               cudaStream_t st) {
+    if (S == 0 || cols == 0) return AJ_OK;
+    if constexpr (sizeof(Tin) == 4 && sizeof(Tout) == 4) {
+        const bool aligned = (cols % 4 == 0) && (ld_x % 4 == 0) && (ld_out % 4 == 0) &&
+                             (reinterpret_cast<uintptr_t>(X) % 16 == 0) && (reinterpret_cast<uintptr_t>(out) % 16 == 0);
+        if (aligned) {
+            dim3 grid((unsigned)S, (unsigned)((cols / 4 + 255) / 256));
+            csc_spmm_t_f32x4_kernel<<<grid, 256, 0, st>>>(c.colptr, c.rows, c.vals, X, ld_x, cols, out, ld_out);
+            return check_launch();
+        }
+    }
+    constexpr int V = 2;
+    dim3 grid((unsigned)S, (unsigned)((cols + 256 * V - 1) / (256 * V)));
+    csc_spmm_t_kernel<Tin, Tout, V><<<grid, 256, 0, st>>>(c.colptr, c.rows, c.vals, X, ld_x, cols, out, ld_out);
+    return check_launch();
+}
+
+template int csc_spmm_t<double, double>(const Csc&, int64_t, const double*, int64_t, int64_t, double*, int64_t,
+                                        cudaStream_t);
+template int csc_spmm_t<float, float>(const Csc&, int64_t, const float*, int64_t, int64_t, float*, int64_t,
+                                      cudaStream_t);
+template int csc_spmm_t<float, double>(const Csc&, int64_t, const float*, int64_t, int64_t, double*, int64_t,
+                                       cudaStream_t);
+
+int csc_spmv_t(const Csc& c, int64_t S, const double* x, double* out, cudaStream_t st) {
+    csc_spmv_t_kernel<<<blocks_for(S, 256, 4 * num_sms()), 256, 0, st>>>(c.colptr, c.rows, c.vals, S, x, out);
+    return check_launch();
+}
+
+template <typename T>
+int csc_compact_tw(const Csc& c, int64_t S, const double* w_compact, int64_t N, const int64_t* native, int64_t M,
+                   T* TW, int* info, cudaStream_t st) {
+    const size_t tab_bytes = sizeof(T) * N * (2 * N - 1);
+    const int64_t items = S * ((M + 1023) / 1024);
+    const size_t smem_cap = 200 * 1024;
+    if (tab_bytes <= smem_cap) {
+        static bool set[2][64] = {};
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (dev < 64 && !set[sizeof(T) == 8][dev]) {
+            if (cudaFuncSetAttribute(csc_compact_tw_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem_cap) != cudaSuccess)
+                return AJ_ERR_CUDA;
+            set[sizeof(T) == 8][dev] = true;
+        }
+        const int per_sm = tab_bytes <= 100 * 1024 ? 2 : 1;
+        int64_t g = (int64_t)num_sms() * per_sm;
+        if (g > items) g = items;
+        csc_compact_tw_kernel<T, true><<<(unsigned)g, 256, tab_bytes, st>>>(c.colptr, c.rows, c.vals, S, w_compact, N,
+                                                                            native, M, TW, info);
+    } else {
+        int64_t g = (int64_t)num_sms() * 4;
+        if (g > items) g = items;
+        csc_compact_tw_kernel<T, false><<<(unsigned)g, 256, 0, st>>>(c.colptr, c.rows, c.vals, S, w_compact, N, native,
+                                                                     M, TW, info);
+    }
+    return check_launch();
+}
+
+template int csc_compact_tw<double>(const Csc&, int64_t, const double*, int64_t, const int64_t*, int64_t, double*, int*,
+                                    cudaStream_t);
+template int csc_compact_tw<float>(const Csc&, int64_t, const double*, int64_t, const int64_t*, int64_t, float*, int*,
+                                   cudaStream_t);
+
+}  // namespace aj
+
+using namespace aj;
+
+namespace {
+
+// F = T^T (T^T X^T)^T for a symmetric-or-not M x M X: TW = T^T X, Omega = TW^T, F = T^T Omega.
+int curvature_from_square(const Csc& c, int64_t S, const double* X, int64_t M, double* TW, double* Om, double* out,
+                          cudaStream_t st) {
+    AJ_TRY(csc_spmm_t<double, double>(c, S, X, M, M, TW, M, st));
+    AJ_TRY(transpose<double>(TW, S, M, Om, st));
+    return csc_spmm_t<double, double>(c, S, Om, S, S, out, S, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+int aj_mapping_matrix(const int64_t* pix_indexes, const double* pix_weights, int64_t M, int64_t B, int64_t S,
+                      double* out, int* info, void* stream) {
+    if (M < 0 || B < 0 || S < 0) return AJ_ERR_ARG;
+    if (M == 0 || S == 0) return AJ_OK;
+    if (!out || (B > 0 && (!pix_indexes || !pix_weights))) return AJ_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    if (cudaMemsetAsync(out, 0, sizeof(double) * M * S, st) != cudaSuccess) return AJ_ERR_CUDA;
+    if (B == 0) return AJ_OK;
+    mapping_dense_kernel<<<blocks_for(M, 128, 8 * num_sms()), 128, 0, st>>>(pix_indexes, pix_weights, M, B, S, out,
+                                                                          info);
+    return check_launch();
+}
+
+int aj_mapping_matrix_original(const int64_t* pix_indexes, const int64_t* pix_sizes, const double* pix_weights,
+                               int64_t n_sub, int64_t B, int64_t S, int64_t M, const int64_t* slim_index,
+                               const double* sub_fraction, double* out, int* info, void* stream) {
+    if (n_sub < 0 || B < 0 || S < 0 || M < 0) return AJ_ERR_ARG;
+    if (M == 0 || S == 0) return AJ_OK;
+    if (!out) return AJ_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    if (cudaMemsetAsync(out, 0, sizeof(double) * M * S, st) != cudaSuccess) return AJ_ERR_CUDA;
+    if (n_sub == 0 || B == 0) return AJ_OK;
+    if (!pix_indexes || !pix_sizes || !pix_weights || !slim_index || !sub_fraction) return AJ_ERR_ARG;
+    mapping_original_kernel<<<blocks_for(n_sub, 128, 8 * num_sms()), 128, 0, st>>>(
+        pix_indexes, pix_sizes, pix_weights, n_sub, B, S, M, slim_index, sub_fraction, out, info);
+    return check_launch();
+}
+
+int aj_data_vector(const double* mapping_matrix, const double* dirty_image, int64_t M, int64_t S, double* out,
+                   void* stream) {
+    if (M < 0 || S < 0) return AJ_ERR_ARG;
+    if (S == 0) return AJ_OK;
+    if (!out || (M > 0 && (!mapping_matrix || !dirty_image))) return AJ_ERR_ARG;
+    data_vector_dense_kernel<<<blocks_for(S, 32), 256, 0, as_stream(stream)>>>(mapping_matrix, dirty_image, M, S, out);
+    return check_launch();
+}
+
+size_t aj_curvature_dense_workspace_size(int64_t M, int64_t S) { return align_up(sizeof(double) * M * S); }
+
+int aj_curvature_dense(const double* w_tilde, const double* mapping_matrix, int64_t M, int64_t S, double* out,
+                       void* workspace, size_t workspace_bytes, void* stream) {
+    if (M < 0 || S < 0) return AJ_ERR_ARG;
+    if (S == 0) return AJ_OK;
+    if (!out || (M > 0 && (!w_tilde || !mapping_matrix))) return AJ_ERR_ARG;
+    if (workspace_bytes < aj_curvature_dense_workspace_size(M, S) || (M > 0 && !workspace)) return AJ_ERR_WORKSPACE;
+    cudaStream_t st = as_stream(stream);
+    double* WT = static_cast<double*>(workspace);
+    // numba.py:435: T^T (W T)
+    AJ_TRY(gemm_f64(false, false, M, S, M, 1.0, w_tilde, M, mapping_matrix, S, 0.0, WT, S, false, st));
+    return gemm_f64(true, false, S, S, M, 1.0, mapping_matrix, S, WT, S, 0.0, out, S, false, st);
+}
+
+size_t aj_sparse_workspace_size(int64_t M, int64_t B, int64_t S, int64_t cols) {
+    Sizer s;
+    s.take<char>(csc_bytes(M, B, S));
+    s.take<double>(S * (cols > M ? cols : M));  // TW
+    s.take<double>((M > S ? M : S) * (cols > S ? cols : S));  // Omega / transposes
+    return s.total();
+}
+
+int aj_sparse_mapping_matrix_transpose_matmul(const double* matrix, int64_t M, int64_t cols,
+                                              const int64_t* pix_indexes, const double* pix_weights, int64_t B,
+                                              int64_t S, double* out, void* workspace, size_t workspace_bytes,
+                                              int* info, void* stream) {
+    if (M < 0 || cols < 0 || B < 0 || S < 0) return AJ_ERR_ARG;
+    if (S == 0 || cols == 0) return AJ_OK;
+    if (!out || (M > 0 && (!matrix || (B > 0 && (!pix_indexes || !pix_weights))))) return AJ_ERR_ARG;
+    if (!workspace || workspace_bytes < csc_bytes(M, B, S)) return AJ_ERR_WORKSPACE;
+    cudaStream_t st = as_stream(stream);
+    Carver cv(workspace, workspace_bytes);
+    Csc c;
+    csc_take(cv, M, B, S, c);
+    AJ_TRY(csc_build(pix_indexes, pix_weights, nullptr, M, B, S, CSC_SUM, c, info, st));
+    return csc_spmm_t<double, double>(c, S, matrix, cols, cols, out, cols, st);
+}
+
+int aj_curvature_w_tilde_sparse(const double* w_tilde, int64_t M, const int64_t* pix_indexes,
+                                const double* pix_weights, int64_t B, int64_t S, double* out, void* workspace,
+                                size_t workspace_bytes, int* info, void* stream) {
+    if (M < 0 || B < 0 || S < 0) return AJ_ERR_ARG;
+    if (S == 0) return AJ_OK;
+    if (!out || (M > 0 && (!w_tilde || !pix_indexes || !pix_weights))) return AJ_ERR_ARG;
+    if (!workspace || workspace_bytes < aj_sparse_workspace_size(M, B, S, M)) return AJ_ERR_WORKSPACE;
+    cudaStream_t st = as_stream(stream);
+    Carver cv(workspace, workspace_bytes);
+    Csc c;
+    csc_take(cv, M, B, S, c);
+    double* TW = cv.take<double>(S * M);
+    double* Om = cv.take<double>(M * S);
+    AJ_TRY(csc_build(pix_indexes, pix_weights, nullptr, M, B, S, CSC_SUM, c, info, st));
+    return curvature_from_square(c, S, w_tilde, M, TW, Om, out, st);
+}
+
+int aj_w_compact_matmul_sparse(const double* w_compact, int64_t N, const int64_t* native_index, int64_t M,
+                               const int64_t* pix_indexes, const double* pix_weights, int64_t B, int64_t S,
+                               double* out, void* workspace, size_t workspace_bytes, int* info, void* stream) {
+    if (N <= 0 || M < 0 || B < 0 || S < 0) return AJ_ERR_ARG;
+    if (M == 0 || S == 0) return AJ_OK;
+    if (!out || !w_compact || !native_index || !pix_indexes || !pix_weights) return AJ_ERR_ARG;
+    if (!workspace || workspace_bytes < aj_sparse_workspace_size(M, B, S, M)) return AJ_ERR_WORKSPACE;
+    cudaStream_t st = as_stream(stream);
+    Carver cv(workspace, workspace_bytes);
+    Csc c;
+    csc_take(cv, M, B, S, c);
+    double* TW = cv.take<double>(S * M);
+    AJ_TRY(csc_build(pix_indexes, pix_weights, nullptr, M, B, S, CSC_SUM, c, info, st));
+    AJ_TRY(csc_compact_tw<double>(c, S, w_compact, N, native_index, M, TW, info, st));
+    return transpose<double>(TW, S, M, out, st);
+}
+
+int aj_curvature_w_compact_sparse(const double* w_compact, int64_t N, const int64_t* native_index, int64_t M,
+                                  const int64_t* pix_indexes, const double* pix_weights, int64_t B, int64_t S,
+                                  double* out, void* workspace, size_t workspace_bytes, int* info, void* stream) {
+    if (N <= 0 || M < 0 || B < 0 || S < 0) return AJ_ERR_ARG;
+    if (S == 0) return AJ_OK;
+    if (!out) return AJ_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    if (M == 0) return cudaMemsetAsync(out, 0, sizeof(double) * S * S, st) == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+    if (!w_compact || !native_index || !pix_indexes || !pix_weights) return AJ_ERR_ARG;
+    if (!workspace || workspace_bytes < aj_sparse_workspace_size(M, B, S, M)) return AJ_ERR_WORKSPACE;
+    Carver cv(workspace, workspace_bytes);
+    Csc c;
+    csc_take(cv, M, B, S, c);
+    double* TW = cv.take<double>(S * M);
+    double* Om = cv.take<double>(M * S);
+    AJ_TRY(csc_build(pix_indexes, pix_weights, nullptr, M, B, S, CSC_SUM, c, info, st));
+    AJ_TRY(csc_compact_tw<double>(c, S, w_compact, N, native_index, M, TW, info, st));
+    AJ_TRY(transpose<double>(TW, S, M, Om, st));
+    return csc_spmm_t<double, double>(c, S, Om, S, S, out, S, st);
+}
+
+size_t aj_curvature_preload_original_workspace_size(int64_t M, int64_t B, int64_t S) {
+    Sizer need;
+    need.take<char>(aj_sparse_workspace_size(M, B, S, M));
+    need.take<double>(M * M);
+    return need.total();
+}
+
+int aj_curvature_preload_original(const double* preload, int64_t py, int64_t px, const int64_t* pix_indexes,
+                                  const int64_t* pix_sizes, const double* pix_weights, int64_t B,
+                                  const int64_t* native_index, int64_t M, int64_t S, double* out,
+                                  void* workspace, size_t workspace_bytes, int* info, void* stream) {
+    if (py <= 0 || px <= 0 || M < 0 || B < 0 || S < 0) return AJ_ERR_ARG;
+    if (S == 0) return AJ_OK;
+    if (!out) return AJ_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    if (M == 0) return cudaMemsetAsync(out, 0, sizeof(double) * S * S, st) == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+    if (!preload || !native_index || !pix_indexes || !pix_sizes || !pix_weights) return AJ_ERR_ARG;
+    if (!workspace || workspace_bytes < aj_curvature_preload_original_workspace_size(M, B, S)) return AJ_ERR_WORKSPACE;
+    Carver cv(workspace, workspace_bytes);
+    Csc c;
+    csc_take(cv, M, B, S, c);
+    double* TW = cv.take<double>(S * M);
+    double* Om = cv.take<double>(M * S);
+    double* W = cv.take<double>(M * M);
+    AJ_TRY(csc_build(pix_indexes, pix_weights, pix_sizes, M, B, S, CSC_SUM, c, info, st));
+    // original.py's upper pairs + mirror + diagonal == T^T W_sym T with W_sym[i][j] = preload[yb-ya][xb-xa]
+    dim3 grid(blocks_for(M, 256, 64), (unsigned)(M < 65535 ? M : 65535));
+    expand_preload_sym_kernel<<<grid, 256, 0, st>>>(preload, py, px, native_index, M, W, info);
+    AJ_LAUNCHED();
+    return curvature_from_square(c, S, W, M, TW, Om, out, st);
+}
+
+int aj_constant_regularization(double coefficient, const int64_t* neighbors, const int64_t* neighbors_sizes,
+                               int64_t S, int64_t P, double* out, int* info, void* stream) {
+    if (S < 0 || P < 0) return AJ_ERR_ARG;
+    if (S == 0) return AJ_OK;
+    if (!out || !neighbors_sizes || (P > 0 && !neighbors)) return AJ_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    if (cudaMemsetAsync(out, 0, sizeof(double) * S * S, st) != cudaSuccess) return AJ_ERR_CUDA;
+    regularization_kernel<<<blocks_for(S, 128, 8 * num_sms()), 128, 0, st>>>(coefficient, nullptr, neighbors,
+                                                                           neighbors_sizes, S, P, out, info);
+    return check_launch();
+}
+
+}  // extern "C"

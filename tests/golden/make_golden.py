@@ -328,8 +328,35 @@ def make_edge(rng_seed: int = 7):
     }
 
 
+def write_signatures(ref_numba, ref_original):
+    """Parameter lists of every public function of numba.py and original.py (util/mod_diff.py:25-57 idea)."""
+    import inspect
+    import json
+
+    out = {}
+    for modname, mod in (("numba", ref_numba), ("original", ref_original)):
+        sigs = {}
+        for name, obj in vars(mod).items():
+            if callable(obj) and getattr(obj, "__module__", "") == mod.__name__:
+                sigs[name] = list(inspect.signature(obj).parameters)
+        # module-level aliases (numba.py:651-653)
+        for name, obj in vars(mod).items():
+            if callable(obj) and name not in sigs and getattr(obj, "__module__", "") == mod.__name__:
+                sigs[name] = list(inspect.signature(obj).parameters)
+        if modname == "numba":
+            sigs["curvature_matrix_via_w_tilde_curvature_preload_interferometer_from"] = list(
+                inspect.signature(mod.curvature_matrix_via_w_tilde_curvature_preload_interferometer_from).parameters
+            )
+        out[modname] = dict(sorted(sigs.items()))
+    (HERE / "reference_signatures.json").write_text(json.dumps(out, indent=1) + "\n")
+    print("wrote reference_signatures.json", flush=True)
+
+
 def main(ref_root: str):
     ref_numba, ref_original = _import_reference(Path(ref_root))
+    write_signatures(ref_numba, ref_original)
+    if "--signatures-only" in sys.argv:
+        return
     from oracle import refdata
     from autojax_gb300 import synthetic
 
@@ -358,4 +385,5 @@ def main(ref_root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    main(args[0] if args else "/root/reference")

@@ -79,8 +79,10 @@ def full_inputs(case: str) -> dict:
 
 
 def call(func, d: dict, **extra):
+    """Call ``func`` with its positional parameters looked up by name in ``d`` (tests.py:564-567)."""
     sig = inspect.signature(func)
-    args = [d[k] for k in sig.parameters if k in d and k not in extra]
+    pos = (inspect.Parameter.POSITIONAL_ONLY, inspect.Parameter.POSITIONAL_OR_KEYWORD)
+    args = [d[k] for k, p in sig.parameters.items() if p.kind in pos and k in d and k not in extra]
     return func(*args, **extra)
 
 
