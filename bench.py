@@ -1,0 +1,530 @@
+#!/usr/bin/env python
+"""Benchmark: log-evidence + gradient evaluations per second on one GB300.
+
+Workload (the K = 1e6 configuration): K = 1,000,000 visibilities, a 100 x 100
+image grid at 0.04" with a 2.4" circular mask (M = 9,504 image pixels),
+S = 1,500 Delaunay source pixels (3 barycentric weights per image pixel).
+w_tilde (M x M, float64) is precomputed once and shared by every evaluation,
+as in the reference (numba.py:814).  One step = one lens-model evaluation:
+logE (numba.py:761-857) and its adjoint (dlogE/dlambda, dlogE/dweights), with
+the regularisation coefficient cycling through lambda in {1e-3, 1e-1, 1e1, 1e3}.
+
+Inputs are synthetic with the configuration's shapes and distributions (the
+reference's dataset is not public); w_tilde alone (722 MB) exceeds L2
+(129 MB), so no explicit L2 flush is needed between steps.
+
+`--impl reference` times the reference's algorithm on the host cores: the
+NumPy restatement of numba.py (the oracle) for logE plus the closed-form
+adjoint, on the same shapes (w_tilde is built from a visibility sample, since
+its values do not change the per-evaluation cost).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT, ROOT / "python-autojax_gb300"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+import numpy as np  # noqa: E402
+
+LAMBDAS = (1e-3, 1e-1, 1e1, 1e3)
+METRIC = "logE+grad evals/s (mixed precision; K=1e6, M=9504, S=1500)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    ap.add_argument("--config", default="cfg3")
+    ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
+    ap.add_argument("--skip-wtilde", action="store_true", help="omit the w_tilde kernel measurement")
+    ap.add_argument("--stages", action="store_true", help="also time the pipeline stages separately")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ helpers
+
+
+class Dist:
+    def __init__(self, gpus: int):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            backend = "nccl"
+            import torch
+
+            if torch.cuda.is_available():
+                torch.cuda.set_device(self.local)
+            else:
+                backend = "gloo"
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg is not None:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if self.pg is None:
+            return x
+        import torch
+
+        dev = torch.device("cuda", self.local) if torch.cuda.is_available() else torch.device("cpu")
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg is not None:
+            self.pg.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        out_dir = ROOT / "gpurun_out" if (ROOT / "gpurun_out").is_dir() else Path(tempfile.gettempdir())
+        self.path = out_dir / f"clocks_{os.getpid()}.csv"
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ("active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names[1:], parts[5:9]):
+                if val.lower() in ("active", "1", "0x1"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            pass
+    return {}
+
+
+_DATASETS: dict = {}
+
+
+def dataset(name: str):
+    from autojax_gb300 import synthetic
+
+    if name not in _DATASETS:
+        _DATASETS[name] = synthetic.make_dataset(name)
+    return _DATASETS[name]
+
+
+def models(d: dict, n: int = len(LAMBDAS)):
+    """The per-step lens models: the dataset's mapping and mesh with the lambda schedule."""
+    return [(d["pix_indexes_for_sub_slim_index"], d["pix_weights_for_sub_slim_index"], d["neighbors"],
+             d["neighbors_sizes"], float(np.sqrt(lam))) for lam in LAMBDAS[:n]]
+
+
+# --------------------------------------------------------------- GPU arm
+
+
+def fma_peak_tflops(precision: int) -> float:
+    """FMA issue rate of this GPU (a register-only probe kernel of the library)."""
+    import torch
+
+    from autojax_gb300 import _lib
+
+    lib = _lib.load()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks = sms * 8
+    iters = 20000 if precision == _lib.AJ_MIXED else 400
+    out = torch.empty(blocks * 256, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream()
+    lib.aj_probe_fma(precision, blocks, 10, out.data_ptr(), st.cuda_stream)
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        _lib.check(lib.aj_probe_fma(precision, blocks, iters, out.data_ptr(), st.cuda_stream), "aj_probe_fma")
+        e1.record(st)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = max(best, 2.0 * 128 * iters * blocks * 256 / (ms * 1e-3) / 1e12)
+    return best
+
+
+def time_region(fn, steps: int, dist: Dist, name: str = "region") -> float:
+    """Max over ranks of the CUDA-event time of `steps` calls of fn (barrier + synchronize on both sides).
+
+    The region is an NVTX range ``bench:<name>`` so a profiler can keep only its launches.
+    """
+    import torch
+
+    dist.barrier()
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push(f"bench:{name}")
+    e0.record(st)
+    for i in range(steps):
+        fn(i)
+    e1.record(st)
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
+    dist.barrier()
+    return dist.max(e0.elapsed_time(e1) / 1e3)
+
+
+def gpu_arm(args, dist: Dist) -> dict:
+    import torch
+
+    import autojax_gb300 as aj
+    from autojax_gb300 import _lib
+    from autojax_gb300.inversion import LogEvidence
+
+    torch.cuda.set_device(dist.local)
+    lib = _lib.load()
+    d = dataset(args.config)
+    M, K, S = d["M"], d["K"], d["S"]
+    dev = torch.device("cuda", dist.local)
+    # shared w_tilde (float64), built on the device from the compact table and expanded
+    noise_real = torch.from_numpy(d["noise_map_real"]).to(dev)
+    uv = torch.from_numpy(d["uv_wavelengths"]).to(dev)
+    w_compact = aj.w_compact_curvature_interferometer_from(d["grid_size"], noise_real, uv, d["pixel_scale"])
+    native = torch.from_numpy(d["native_index_for_slim_index"]).to(dev)
+    w_tilde = aj.w_tilde_via_compact_from(w_compact, native)
+    torch.cuda.synchronize()
+    B, P = d["pix_indexes_for_sub_slim_index"].shape[1], d["neighbors"].shape[1]
+    common = dict(S=S, B=B, P=P, with_grad=True, device=dev)
+    ev = {prec: LogEvidence(d["dirty_image"], d["data"], d["noise_map"], w_tilde, precision=prec, **common)
+          for prec in ("mixed", "fp64")}
+    mods = models(d)
+    for e in ev.values():
+        e.set_model(*mods[0][:4], coefficient=mods[0][4])
+        if not args.no_graph:
+            e.capture()
+    coefs = [torch.full((1,), m[4], dtype=torch.float64, device=dev) for m in mods]
+
+    def stepper(e):
+        def f(i):
+            e.coefficient.copy_(coefs[i % len(coefs)])
+            e.step()
+        return f
+
+    # accuracy of the mixed path against the float64 path over the lambda schedule
+    rel = []
+    for c in coefs:
+        vals = {}
+        for prec, e in ev.items():
+            e.coefficient.copy_(c)
+            e.step()
+            torch.cuda.synchronize()
+            e.check()
+            vals[prec] = e.out.cpu().numpy().copy()
+        rel.append(abs(vals["mixed"][0] - vals["fp64"][0]) / abs(vals["fp64"][0]))
+
+    for e in ev.values():
+        f = stepper(e)
+        for i in range(args.warmup):
+            f(i)
+    torch.cuda.synchronize()
+
+    clk = ClockSampler(dist.local)
+    clk.start()
+    t_mixed = time_region(stepper(ev["mixed"]), args.steps, dist, "timed_mixed")
+    clocks = clk.stop()
+    t_fp64 = time_region(stepper(ev["fp64"]), args.steps, dist, "timed_fp64")
+    ev["mixed"].check()
+
+    # end to end through the public evaluator: host NumPy inputs -> pinned H2D -> evaluation -> D2H
+    e = ev["mixed"]
+    for i in range(args.warmup):
+        e.evaluate_host(*mods[i % len(mods)])
+    dist.barrier()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        e.evaluate_host(*mods[i % len(mods)])
+    t_e2e = dist.max(time.perf_counter() - t0)
+
+    # roofline of the dominant kernel group: the float64 blocked Cholesky / inverse (measured standalone)
+    A = torch.from_numpy(aj.constant_regularization_matrix_from(1.0, d["neighbors"], d["neighbors_sizes"])).to(dev)
+    F = aj.curvature_matrix_via_w_wilde_sparse_mapping_matrix_from(
+        w_tilde, torch.from_numpy(d["pix_indexes_for_sub_slim_index"]).to(dev),
+        torch.from_numpy(d["pix_weights_for_sub_slim_index"]).to(dev), S)
+    A = (A + F).contiguous()
+    ws = torch.empty(lib.aj_spd_inverse_workspace_size(S), dtype=torch.uint8, device=dev)
+    Ainv = torch.empty((S, S), dtype=torch.float64, device=dev)
+    ld = torch.empty(1, dtype=torch.float64, device=dev)
+    info = torch.zeros(2, dtype=torch.int32, device=dev)
+    stc = torch.cuda.current_stream().cuda_stream
+
+    def inv_call(i):
+        _lib.check(lib.aj_spd_inverse(A.data_ptr(), S, Ainv.data_ptr(), ld.data_ptr(), ws.data_ptr(), ws.numel(),
+                                      info.data_ptr(), stc), "aj_spd_inverse")
+
+    def chol_call(i):
+        _lib.check(lib.aj_spd_logdet(A.data_ptr(), S, ld.data_ptr(), ws.data_ptr(), ws.numel(), info.data_ptr(), stc),
+                   "aj_spd_logdet")
+
+    for i in range(2):
+        inv_call(i)
+    reps = 5
+    t_chol = time_region(chol_call, reps, dist) / reps
+    t_inv = time_region(inv_call, reps, dist) / reps
+    fp64_peak = fma_peak_tflops(_lib.AJ_FP64)
+    fp32_peak = fma_peak_tflops(_lib.AJ_MIXED)
+    # algorithmic flops: Cholesky S^3/3, triangular inverse S^3/3, L^-T L^-1 S^3/3
+    chol_flops = S**3 / 3.0
+    inv_flops = S**3
+    achieved = inv_flops / t_inv / 1e12
+
+    result = {
+        "metric": METRIC,
+        "value": args.steps * dist.world / t_mixed,
+        "unit": "evals/s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_mixed / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded; shapes and distributions of the K=1e6 configuration)",
+        "config": {
+            "workload": f"{args.config}: K={K} visibilities, M={M} image pixels (100x100 at 0.04\", r=2.4\"), "
+                        f"S={S} Delaunay source pixels, B={B}; w_tilde precomputed (float64, resident)",
+            "lambdas": list(LAMBDAS),
+            "l2": "inputs larger than L2 (w_tilde 722 MB float64 re-read every step)",
+            "graph": not args.no_graph,
+            "parallelism": f"replicas x{dist.world}",
+        },
+        "fp64_path": {"value": args.steps * dist.world / t_fp64, "ms_per_step": 1e3 * t_fp64 / args.steps},
+        "mixed_over_fp64": t_fp64 / t_mixed,
+        "max_rel_dlogE_mixed_vs_fp64": max(rel),
+        "e2e": {"value": args.steps * dist.world / t_e2e, "unit": "evals/s", "h2d_bytes_per_step": e.h2d_bytes(),
+                "d2h_bytes_per_step": e.d2h_bytes()},
+        "gpu_launches": (ev["mixed"].launches_per_eval or 0) * args.steps,
+        "roofline": {
+            "kernel": "blocked float64 Cholesky + triangular inverse + L^-T L^-1 (aj_spd_inverse; gemm_f64 tiles)",
+            "bound": "fp64",
+            "achieved": achieved,
+            "peak": fp64_peak,
+            "unit": "TFLOP/s",
+            "frac": achieved / fp64_peak,
+            "peak_source": "measured in this run (aj_probe_fma float64 FMA loop)",
+            "traffic": None,
+            "cholesky_ms": 1e3 * t_chol,
+            "cholesky_tflops": chol_flops / t_chol / 1e12,
+            "inverse_ms": 1e3 * t_inv,
+        },
+        "peaks": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak,
+                  "hbm_gbs": measured_peaks().get("hbm_gbs"), "bf16_tflops": measured_peaks().get("bf16_tflops")},
+        "clocks": clocks,
+    }
+    if not args.skip_wtilde:
+        result["w_tilde"] = wtilde_bench(d, dev, fp32_peak)
+    if args.stages:
+        result["stages_ms"] = stage_times(d, w_tilde, dev, dist)
+    return result
+
+
+def wtilde_bench(d, dev, fp32_peak) -> dict:
+    """Direct w_tilde kernel (numba.py:156-207) on the workload's M with a visibility sample."""
+    import torch
+
+    from autojax_gb300 import _lib
+
+    lib = _lib.load()
+    Ks = 16384
+    g = torch.from_numpy(d["grid_radians_slim"]).to(dev)
+    uv = torch.from_numpy(d["uv_wavelengths"][:Ks].copy()).to(dev)
+    n = torch.from_numpy(d["noise_map_real"][:Ks].copy()).to(dev)
+    M = g.shape[0]
+    out = {}
+    for name, pc in (("mixed", _lib.AJ_MIXED),):
+        W = torch.empty((M, M), dtype=torch.float64, device=dev)
+        ws = torch.empty(lib.aj_w_tilde_curvature_workspace_size(Ks, M, pc), dtype=torch.uint8, device=dev)
+        st = torch.cuda.current_stream()
+
+        def call():
+            _lib.check(lib.aj_w_tilde_curvature(n.data_ptr(), uv.data_ptr(), g.data_ptr(), Ks, M, W.data_ptr(), None,
+                                                ws.data_ptr(), ws.numel(), pc, st.cuda_stream), "aj_w_tilde_curvature")
+
+        call()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        call()
+        e1.record(st)
+        e1.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        terms = M * (M + 1) / 2 * Ks
+        # the symmetric product does 2 FMA (4 flops) per unique (pair, visibility) term
+        flops = 4.0 * terms
+        out[name] = {"K_sample": Ks, "M": M, "seconds": sec, "terms_per_s": terms / sec,
+                     "fp32_tflops": flops / sec / 1e12, "fp32_frac": flops / sec / 1e12 / fp32_peak}
+    return out
+
+
+def stage_times(d, w_tilde, dev, dist) -> dict:
+    import torch
+
+    import autojax_gb300 as aj
+
+    idx = torch.from_numpy(d["pix_indexes_for_sub_slim_index"]).to(dev)
+    w = torch.from_numpy(d["pix_weights_for_sub_slim_index"]).to(dev)
+    S = d["S"]
+    out = {}
+    for name, fn in (
+        ("curvature_sparse_f64", lambda i: aj.curvature_matrix_via_w_wilde_sparse_mapping_matrix_from(w_tilde, idx, w, S)),
+        ("regularization", lambda i: aj.constant_regularization_matrix_from(1.0, torch.from_numpy(d["neighbors"]).to(dev),
+                                                                            torch.from_numpy(d["neighbors_sizes"]).to(dev))),
+    ):
+        fn(0)
+        out[name] = 1e3 * time_region(fn, 3, dist) / 3
+    return out
+
+
+# -------------------------------------------------------------- CPU legs
+
+
+def cpu_eval_setup(d: dict, k_sample: int = 20000):
+    """w_tilde for the host arm from a visibility sample (its values do not change the per-evaluation cost)."""
+    from oracle import numpy_port as ref
+
+    wc = ref.w_compact_curvature_interferometer_from(d["grid_size"], d["noise_map_real"][:k_sample],
+                                                     d["uv_wavelengths"][:k_sample], d["pixel_scale"])
+    return ref.w_tilde_via_compact_from(wc, d["native_index_for_slim_index"])
+
+
+def cpu_time(d: dict, W, evals: int) -> tuple[float, int]:
+    from oracle import adjoint
+
+    mods = models(d)
+    t0 = time.perf_counter()
+    for i in range(evals):
+        idx, w, nb, nsz, c = mods[i % len(mods)]
+        adjoint.log_evidence_and_grad(d["dirty_image"], d["data"], d["noise_map"], W, idx, w, nb, nsz, coefficient=c)
+    return time.perf_counter() - t0, evals
+
+
+def cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline(d: dict, W, budget_s: float = 20.0) -> dict:
+    sec1, _ = cpu_time(d, W, 1)
+    n = max(1, min(20, int(budget_s / max(sec1, 1e-3))))
+    sec, n = cpu_time(d, W, n)
+    return {"value": n / sec, "unit": "evals/s", "cores": cores(), "kind": "port",
+            "sample": f"{n} logE+grad evaluations of the workload's shapes on the host (NumPy port of numba.py "
+                      "logE + closed-form adjoint; w_tilde from a 20000-visibility sample, chi^2 over all K)"}
+
+
+def reference_arm(args, dist: Dist) -> dict:
+    d = dataset(args.config)
+    W = cpu_eval_setup(d)
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_time(d, W, 1)
+    sec, n = cpu_time(d, W, args.steps)
+    v = n / sec
+    return {
+        "metric": METRIC,
+        "impl": "reference",
+        "value": v,
+        "unit": "evals/s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * sec / n,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded; shapes and distributions of the K=1e6 configuration)",
+        "config": {"workload": f"{args.config}: K={d['K']}, M={d['M']}, S={d['S']}; host NumPy port of numba.py",
+                   "lambdas": list(LAMBDAS)},
+        "cpu_baseline": {"value": v, "unit": "evals/s", "cores": cores(), "kind": "port",
+                         "sample": f"{n} logE+grad evaluations (numba.py logE restated in NumPy + closed-form "
+                                   "adjoint); w_tilde from a 20000-visibility sample"},
+        "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    dist = Dist(args.gpus)
+    try:
+        if args.impl == "reference":
+            if dist.rank != 0:
+                return
+            print(json.dumps(reference_arm(args, dist)), flush=True)
+            return
+        res = gpu_arm(args, dist)
+        if dist.rank == 0 and dist.world == 1 and not args.skip_cpu:
+            d = dataset(args.config)
+            res["cpu_baseline"] = cpu_baseline(d, cpu_eval_setup(d))
+        if dist.rank == 0:
+            print(json.dumps(res), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

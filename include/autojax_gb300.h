@@ -194,21 +194,34 @@ int aj_spd_solve(const double* data_vector, const double* A, int64_t S, double* 
 int aj_spd_logdet(const double* A, int64_t S, double* out, void* workspace, size_t workspace_bytes, int* info,
                   void* stream);
 
+/* A^-1 (S, S, full symmetric) of a symmetric positive definite A via its
+ * Cholesky factor: L^-1 by block forward substitution, then L^-T L^-1.
+ * The adjoint of numba.py:849 (d log|A| = tr(A^-1 dA)) needs it; no counterpart. */
+size_t aj_spd_inverse_workspace_size(int64_t S);
+int aj_spd_inverse(const double* A, int64_t S, double* Ainv, double* logdet, void* workspace, size_t workspace_bytes,
+                   int* info, void* stream);
+
 /* numba.py:735-752 noise_normalization_complex_from: *out = 2 (K log 2pi + sum log|Re| + sum log|Im|). */
 int aj_noise_normalization(const double* noise_map_c128, int64_t K, double* out, void* stream);
 
 /* ------------------------------------------------------------ likelihood */
 
+/* Split float64 values into double-float planes: hi = float(x), lo = float(x - hi). */
+int aj_split_f64(const double* x, int64_t n, float* hi, float* lo, void* stream);
+
 /* Dimensions and inputs of one log-evidence evaluation. The shared W (M, M)
- * is w_tilde64 (AJ_FP64) or w_tilde32 (AJ_MIXED); for the compact variant
- * w_compact (N, 2N-1) and native_index (M, 2) replace it. */
+ * is w_tilde64, and for AJ_MIXED also its double-float planes w_tilde_hi /
+ * w_tilde_lo (split once with aj_split_f64; without them the mixed path splits
+ * w_tilde64 on every call); for the compact variant w_compact (N, 2N-1) and
+ * native_index (M, 2) replace it. */
 typedef struct aj_problem {
     int64_t M, K, S, B, P, N;
     const double* dirty_image;       /* (M,) */
     const double* data;              /* (K,) complex128 */
     const double* noise_map;         /* (K,) complex128 */
     const double* w_tilde64;         /* (M, M) or NULL */
-    const float* w_tilde32;          /* (M, M) or NULL */
+    const float* w_tilde_hi;         /* (M, M) double-float planes of w_tilde for AJ_MIXED */
+    const float* w_tilde_lo;         /* (hi + lo = w_tilde; see aj_split_f64), or NULL */
     const double* w_compact;         /* (N, 2N-1) or NULL */
     const int64_t* native_index;     /* (M, 2) or NULL */
     const int64_t* pix_indexes;      /* (M, B) */

@@ -42,7 +42,8 @@ class Problem(C.Structure):
         ("data", P),
         ("noise_map", P),
         ("w_tilde64", P),
-        ("w_tilde32", P),
+        ("w_tilde_hi", P),
+        ("w_tilde_lo", P),
         ("w_compact", P),
         ("native_index", P),
         ("pix_indexes", P),
@@ -88,7 +89,10 @@ SIGNATURES = {
     "aj_spd_solve_workspace_size": (SZ, [I64]),
     "aj_spd_solve": (INT, [P, P, I64, P, P, SZ, P, P]),
     "aj_spd_logdet": (INT, [P, I64, P, P, SZ, P, P]),
+    "aj_spd_inverse_workspace_size": (SZ, [I64]),
+    "aj_spd_inverse": (INT, [P, I64, P, P, P, SZ, P, P]),
     "aj_noise_normalization": (INT, [P, I64, P, P]),
+    "aj_split_f64": (INT, [P, I64, P, P, P]),
     "aj_log_evidence_workspace_size": (SZ, [C.POINTER(Problem), INT, INT]),
     "aj_log_evidence": (INT, [C.POINTER(Problem), INT, INT, P, P, P, P, SZ, P, P]),
 }

@@ -65,6 +65,14 @@ class LogEvidence:
                        if native_index_for_slim_index is not None else None)
         if self.w_tilde is None and (self.w_compact is None or self.native is None):
             raise ValueError("pass w_tilde, or w_compact with native_index_for_slim_index")
+        self.w_hi = self.w_lo = None
+        if self.w_tilde is not None and self.pc == _lib.AJ_MIXED:
+            # double-float planes of w_tilde, split once for every evaluation
+            self.w_hi = torch.empty(self.w_tilde.shape, dtype=torch.float32, device=dev)
+            self.w_lo = torch.empty(self.w_tilde.shape, dtype=torch.float32, device=dev)
+            _lib.check(self.lib.aj_split_f64(self.w_tilde.data_ptr(), self.w_tilde.numel(), self.w_hi.data_ptr(),
+                                             self.w_lo.data_ptr(), torch.cuda.current_stream(dev).cuda_stream),
+                       "aj_split_f64")
         # persistent per-model inputs (graph replays read these addresses)
         self.pix_indexes = torch.zeros((self.M, self.B), dtype=torch.int64, device=dev)
         self.pix_weights = torch.zeros((self.M, self.B), dtype=torch.float64, device=dev)
@@ -100,6 +108,9 @@ class LogEvidence:
         p.noise_map = self.noise.data_ptr()
         if self.w_tilde is not None:
             p.w_tilde64 = self.w_tilde.data_ptr()
+            if self.w_hi is not None:
+                p.w_tilde_hi = self.w_hi.data_ptr()
+                p.w_tilde_lo = self.w_lo.data_ptr()
         else:
             p.w_compact = self.w_compact.data_ptr()
             p.native_index = self.native.data_ptr()

@@ -35,6 +35,31 @@ int spd_solve_vec(int64_t S, SpdWorkspace& w, const double* b, double* x, int* i
 // Ainv (S x S, full symmetric) = Linv^T Linv
 int spd_inverse_from_factor(int64_t S, SpdWorkspace& w, double* Ainv, cudaStream_t st);
 
+// ---- linalg_df.cu (double-float planes: hi and lo float arrays)
+
+struct DfSpd {
+    float *Lh, *Ll;  // factor (S x S)
+    float *Ih, *Il;  // inverse factor (S x S) or null
+    float *dh, *dl;  // inverses of the diagonal blocks
+    double* piv;     // the S pivots L_ii in float64
+    double* vec;     // S scratch
+};
+size_t dfspd_bytes(int64_t S, bool with_inverse);
+DfSpd dfspd_carve(Carver& cv, int64_t S, bool with_inverse);
+int df_split(const double* x, int64_t n, float* hi, float* lo, cudaStream_t st);
+int df_join(const float* hi, const float* lo, int64_t n, double* x, cudaStream_t st);
+int df_add_f64(const float* ah, const float* al, const double* b, int64_t n, float* oh, float* ol, cudaStream_t st);
+int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const float* Ah, const float* Al, int64_t lda,
+            const float* Bh, const float* Bl, int64_t ldb, bool accumulate, float* Ch, float* Cl, int64_t ldc,
+            bool lower_only, bool tri_k, cudaStream_t st);
+int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* logdet, int* info, cudaStream_t st);
+int dfspd_invert_factor(int64_t S, DfSpd& w, cudaStream_t st);
+int dfspd_inverse_from_factor(int64_t S, DfSpd& w, float* Ah, float* Al, cudaStream_t st);
+int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st);
+int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x, double* r,
+                        cudaStream_t st);
+int df_frob_lower(const float* h, const float* l, int64_t S, double* partial, int64_t nparts, cudaStream_t st);
+
 // ---- mapping.cu
 
 // H = 1e-8 I + c^2 L (numba.py:686-694); c read from coefficient_dev when it is not null
@@ -46,8 +71,8 @@ struct Csc {
     int* colptr;   // S + 1
     int* rows;     // nnz capacity M * B
     double* vals;  // nnz capacity
-    int* keys;     // scratch, nnz capacity
-    int* cursor;   // S
+    int* keys;     // scratch: per-chunk column histograms
+    int* cursor;   // scratch: per-chunk column write offsets
 };
 enum CscMode { CSC_SUM = 0, CSC_ASSIGN = 1 };
 void csc_take(Carver& cv, int64_t M, int64_t B, int64_t S, Csc& c);
@@ -59,6 +84,9 @@ int csc_build(const int64_t* idx, const double* w, const int64_t* sizes, int64_t
 template <typename Tin, typename Tout>
 int csc_spmm_t(const Csc& c, int64_t S, const Tin* X, int64_t ld_x, int64_t cols, Tout* out, int64_t ld_out,
                cudaStream_t st);
+// double-float planes: out (S x cols) = T^T X with X given as (hi, lo) planes
+int csc_spmm_t_df(const Csc& c, int64_t S, const float* Xh, const float* Xl, int64_t ld_x, int64_t cols, float* Oh,
+                  float* Ol, int64_t ld_out, cudaStream_t st);
 // out[s] = sum_e val[e] * x[row[e]]
 int csc_spmv_t(const Csc& c, int64_t S, const double* x, double* out, cudaStream_t st);
 // TW (S x M) with TW[s][m1] = sum_e val[e] * Wc(m1, row[e]) from the compact table (T float or double)

@@ -19,6 +19,7 @@
 #include <math.h>
 
 #include "aj_internal.cuh"
+#include "df32.cuh"
 
 namespace aj {
 
@@ -57,7 +58,8 @@ __global__ void __launch_bounds__(KT_THREADS)
 // out[0] = logE from the partials, s.D, log|A|, log|H| (numba.py:846-857)
 __global__ void assemble_kernel(const double* __restrict__ partial, int64_t nblk, int64_t K,
                                 const double* __restrict__ s, const double* __restrict__ D, int64_t S,
-                                const double* __restrict__ logdets, double* __restrict__ out) {
+                                const double* __restrict__ logdets, const double* __restrict__ shift,
+                                double* __restrict__ out) {
     __shared__ double red[32];
     double chi2 = 0.0, lg = 0.0, sd = 0.0;
     for (int64_t b = threadIdx.x; b < nblk; b += blockDim.x) {
@@ -70,7 +72,9 @@ __global__ void assemble_kernel(const double* __restrict__ partial, int64_t nblk
     sd = block_sum(sd, red);
     if (threadIdx.x == 0) {
         const double norm = 2.0 * ((double)K * 1.8378770664093454836 + lg);  // log(2 pi)
-        out[0] = -0.5 * (chi2 - sd + logdets[0] - logdets[1] + norm);
+        const double sh = shift ? shift[0] : 0.0;
+        const double logH = logdets[1] + (sh > 0.0 ? log(1e-8) - log(1e-8 + sh) : 0.0);
+        out[0] = -0.5 * (chi2 - sd + logdets[0] - logH + norm);
     }
 }
 
@@ -97,7 +101,8 @@ __global__ void frob_lower_kernel(const double* __restrict__ Li, int64_t S, doub
 __global__ void dlam_kernel(const int64_t* __restrict__ nb, const int64_t* __restrict__ nsz, int64_t S, int64_t P,
                             const double* __restrict__ s, const double* __restrict__ Ainv,
                             const double* __restrict__ frob_partial, int64_t nfrob, double coef,
-                            const double* __restrict__ coef_dev, double* __restrict__ out) {
+                            const double* __restrict__ coef_dev, const double* __restrict__ shift,
+                            double* __restrict__ out) {
     const double c = coef_dev ? *coef_dev : coef;
     const double lam = c * c;
     __shared__ double red[32];
@@ -122,6 +127,8 @@ __global__ void dlam_kernel(const int64_t* __restrict__ nb, const int64_t* __res
     trl = block_sum(trl, red);
     trh = block_sum(trh, red);
     if (threadIdx.x == 0) {
+        const double sh = shift ? shift[0] : 0.0;
+        if (sh > 0.0) trh += 1.0 / 1e-8 - 1.0 / (1e-8 + sh);
         // tr(H^-1 L): (S - eps tr(H^-1)) / lambda, or tr(L) / eps when lambda = 0 (H = eps I)
         const double trHL = lam != 0.0 ? ((double)S - 1e-8 * trh) / lam : trl / 1e-8;
         out[1] = -0.5 * (sls + tra - trHL);
@@ -167,6 +174,68 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Deflation of H's constant mode for the double-float factorisation.
+// When the neighbour lists describe a graph Laplacian (sizes equal to the
+// entries before -1, no self-loops, every entry mirrored with the same
+// multiplicity), H 1 = 1e-8 1 exactly, so H~ = H + (c/S) 1 1^T only moves that
+// eigenvalue from 1e-8 to 1e-8 + c and
+//   log|H| = log|H~| + log(1e-8) - log(1e-8 + c),
+//   tr(H^-1) = tr(H~^-1) + 1/1e-8 - 1/(1e-8 + c).
+// With c = lambda * mean(n) H~ is as well conditioned as lambda L on the
+// complement of the constant vector, where 48-bit arithmetic suffices.
+// Lists that are not a Laplacian get c = 0 (no deflation).
+__global__ void laplacian_shift_kernel(const int64_t* __restrict__ nb, const int64_t* __restrict__ nsz, int64_t S,
+                                       int64_t P, double coef, const double* __restrict__ coef_dev,
+                                       double* __restrict__ shift) {
+    __shared__ int ok_s;
+    __shared__ double red[32];
+    if (threadIdx.x == 0) ok_s = 1;
+    __syncthreads();
+    int ok = 1;
+    double nsum = 0.0;
+    for (int64_t i = threadIdx.x; i < S; i += blockDim.x) {
+        const int64_t* row = nb + i * P;
+        int64_t cnt = 0;
+        for (int64_t j = 0; j < P; ++j) {
+            const int64_t k = row[j];
+            if (k == -1) break;
+            ++cnt;
+            if (k < 0 || k >= S || k == i) {
+                ok = 0;
+                continue;
+            }
+            int64_t m_ik = 0, m_ki = 0;
+            for (int64_t q = 0; q < P && row[q] != -1; ++q) m_ik += row[q] == k;
+            const int64_t* rk = nb + k * P;
+            for (int64_t q = 0; q < P && rk[q] != -1; ++q) m_ki += rk[q] == i;
+            if (m_ik != m_ki) ok = 0;
+        }
+        if (cnt != nsz[i]) ok = 0;
+        nsum += (double)nsz[i];
+    }
+    if (!ok) atomicAnd(&ok_s, 0);
+    nsum = block_sum(nsum, red);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double c = coef_dev ? *coef_dev : coef;
+        const double lam = c * c;
+        const double sh = ok_s ? lam * (nsum / (double)S) : 0.0;
+        shift[0] = sh > 0.0 ? sh : 0.0;
+    }
+}
+
+// (hi, lo) planes of H + shift[0] / S
+__global__ void split_shifted_kernel(const double* __restrict__ H, int64_t S, const double* __restrict__ shift,
+                                     float* __restrict__ hi, float* __restrict__ lo) {
+    const double add = shift[0] / (double)S;
+    const int64_t n = S * S;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const df v = df_from(H[t] + add);
+        hi[t] = v.hi;
+        lo[t] = v.lo;
+    }
+}
+
 // single-block noise normalisation for the standalone drop-in call
 __global__ void noise_norm_kernel(const double* __restrict__ x, int64_t n2, int64_t K, double* __restrict__ out) {
     __shared__ double red[32];
@@ -190,17 +259,22 @@ __global__ void noise_norm_kernel(const double* __restrict__ x, int64_t n2, int6
 
 struct EvidenceBufs {
     Csc ca{}, cs{};
-    SpdWorkspace wa{}, wh{};
-    double *TW, *Om, *F, *H, *A, *Ainv, *D, *s, *kpart, *fpart, *logdets;
+    SpdWorkspace wa{}, wh{};          // float64 path
+    DfSpd da{}, dh{};                 // mixed path
+    double *TW, *Om, *F, *H, *A, *Ainv, *D, *s, *res, *kpart, *fpart, *logdets;
+    float *Wh, *Wl;                   // w_tilde planes when split per call
+    float *TWh, *TWl, *Omh, *Oml, *Fh, *Fl, *Hh, *Hl, *Ah, *Al, *AIh, *AIl;
     int64_t nk_blocks, nfrob;
-    bool compact, grad;
+    bool compact, grad, mixed;
 };
 
 // One routine both sizes (base == nullptr) and carves the workspace, so the two never disagree.
-size_t evidence_carve(const aj_problem* p, bool with_grad, void* base, size_t bytes, EvidenceBufs& b) {
+size_t evidence_carve(const aj_problem* p, bool mixed, bool with_grad, void* base, size_t bytes, EvidenceBufs& b) {
     const int64_t M = p->M, S = p->S, B = p->B;
+    b = EvidenceBufs{};
     b.compact = p->w_compact != nullptr;
     b.grad = with_grad;
+    b.mixed = mixed;
     b.nk_blocks = (2 * p->K + (int64_t)KT_THREADS * KT_PER_THREAD - 1) / ((int64_t)KT_THREADS * KT_PER_THREAD);
     if (b.nk_blocks < 1) b.nk_blocks = 1;
     b.nfrob = 2 * (int64_t)num_sms();
@@ -219,25 +293,58 @@ size_t evidence_carve(const aj_problem* p, bool with_grad, void* base, size_t by
     } else {
         b.cs = b.ca;
     }
-    b.TW = cv.take<double>(S * M);
-    b.Om = cv.take<double>(M * S);
-    b.F = cv.take<double>(S * S);
     b.H = cv.take<double>(S * S);
-    b.A = cv.take<double>(S * S);
-    {
-        Carver c = sub(spd_workspace_bytes(S, with_grad));
-        b.wa = spd_carve(c, S, with_grad);
-    }
-    {
-        Carver c = sub(spd_workspace_bytes(S, with_grad));
-        b.wh = spd_carve(c, S, with_grad);
-    }
-    b.Ainv = with_grad ? cv.take<double>(S * S) : nullptr;
     b.D = cv.take<double>(S);
     b.s = cv.take<double>(S);
+    b.res = cv.take<double>(S);
     b.kpart = cv.take<double>(2 * b.nk_blocks);
     b.fpart = cv.take<double>(b.nfrob);
     b.logdets = cv.take<double>(8);
+    if (!mixed) {
+        b.TW = cv.take<double>(S * M);
+        b.Om = cv.take<double>(M * S);
+        b.F = cv.take<double>(S * S);
+        b.A = cv.take<double>(S * S);
+        {
+            Carver c = sub(spd_workspace_bytes(S, with_grad));
+            b.wa = spd_carve(c, S, with_grad);
+        }
+        {
+            Carver c = sub(spd_workspace_bytes(S, with_grad));
+            b.wh = spd_carve(c, S, with_grad);
+        }
+        b.Ainv = with_grad ? cv.take<double>(S * S) : nullptr;
+    } else {
+        if (!b.compact && !(p->w_tilde_hi && p->w_tilde_lo)) {
+            b.Wh = cv.take<float>(M * M);
+            b.Wl = cv.take<float>(M * M);
+        }
+        if (b.compact) b.TW = cv.take<double>(S * M);
+        b.TWh = cv.take<float>(S * M);
+        b.TWl = cv.take<float>(S * M);
+        b.Omh = cv.take<float>(M * S);
+        b.Oml = cv.take<float>(M * S);
+        b.Fh = cv.take<float>(S * S);
+        b.Fl = cv.take<float>(S * S);
+        b.Hh = cv.take<float>(S * S);
+        b.Hl = cv.take<float>(S * S);
+        b.Ah = cv.take<float>(S * S);
+        b.Al = cv.take<float>(S * S);
+        {
+            Carver c = sub(dfspd_bytes(S, true));
+            b.da = dfspd_carve(c, S, true);
+        }
+        {
+            Carver c = sub(dfspd_bytes(S, with_grad));
+            b.dh = dfspd_carve(c, S, with_grad);
+        }
+        if (with_grad) {
+            b.AIh = cv.take<float>(S * S);
+            b.AIl = cv.take<float>(S * S);
+            b.Ainv = cv.take<double>(S * S);
+            b.Om = cv.take<double>(M * S);
+        }
+    }
     return align_up(cv.used);
 }
 
@@ -268,10 +375,15 @@ int aj_noise_normalization(const double* noise_map_c128, int64_t K, double* out,
 }
 
 size_t aj_log_evidence_workspace_size(const aj_problem* p, int precision, int with_grad) {
-    (void)precision;
     if (check_problem(p) != AJ_OK) return 0;
     EvidenceBufs b;
-    return evidence_carve(p, with_grad != 0, nullptr, 0, b);
+    return evidence_carve(p, precision == AJ_MIXED, with_grad != 0, nullptr, 0, b);
+}
+
+int aj_split_f64(const double* x, int64_t n, float* hi, float* lo, void* stream) {
+    if (n < 0 || (n > 0 && (!x || !hi || !lo))) return AJ_ERR_ARG;
+    if (n == 0) return AJ_OK;
+    return df_split(x, n, hi, lo, as_stream(stream));
 }
 
 int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* out, double* grad_weights,
@@ -279,10 +391,11 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
     AJ_TRY(check_problem(p));
     if (precision != AJ_FP64 && precision != AJ_MIXED) return AJ_ERR_ARG;
     if (!out || (with_grad && !grad_weights)) return AJ_ERR_ARG;
+    const bool mixed = precision == AJ_MIXED;
     EvidenceBufs b;
-    const size_t need = evidence_carve(p, with_grad != 0, nullptr, 0, b);
+    const size_t need = evidence_carve(p, mixed, with_grad != 0, nullptr, 0, b);
     if (!workspace || workspace_bytes < need) return AJ_ERR_WORKSPACE;
-    evidence_carve(p, with_grad != 0, workspace, workspace_bytes, b);
+    evidence_carve(p, mixed, with_grad != 0, workspace, workspace_bytes, b);
     cudaStream_t st = as_stream(stream);
     const int64_t M = p->M, S = p->S, B = p->B, K = p->K;
 
@@ -290,22 +403,49 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
     AJ_TRY(csc_build(p->pix_indexes, p->pix_weights, nullptr, M, B, S, CSC_ASSIGN, b.ca, info, st));
     if (b.compact) AJ_TRY(csc_build(p->pix_indexes, p->pix_weights, nullptr, M, B, S, CSC_SUM, b.cs, info, st));
     AJ_TRY(csc_spmv_t(b.ca, S, p->dirty_image, b.D, st));
-
-    // Omega = W T (via TW = T^T W, W symmetric), F = T^T Omega
-    if (b.compact)
-        AJ_TRY(csc_compact_tw<double>(b.cs, S, p->w_compact, p->N, p->native_index, M, b.TW, info, st));
-    else
-        AJ_TRY(csc_spmm_t<double, double>(b.cs, S, p->w_tilde64, M, M, b.TW, M, st));
-    AJ_TRY(transpose<double>(b.TW, S, M, b.Om, st));
-    AJ_TRY(csc_spmm_t<double, double>(b.cs, S, b.Om, S, S, b.F, S, st));
-
-    // H, A = F + H, factorisations and log-determinants
     AJ_TRY(regularization(p->coefficient, p->coefficient_dev, p->neighbors, p->neighbors_sizes, S, p->P, b.H, info, st));
-    add_kernel<<<blocks_for(S * S, 256, 8 * num_sms()), 256, 0, st>>>(b.F, b.H, b.A, S * S);
-    AJ_LAUNCHED();
-    AJ_TRY(spd_factor(b.A, S, b.wa, b.logdets + 0, info, st));
-    AJ_TRY(spd_factor(b.H, S, b.wh, b.logdets + 1, info, st));
-    AJ_TRY(spd_solve_vec(S, b.wa, b.D, b.s, info, st));
+
+    if (!mixed) {
+        // Omega = W T (via TW = T^T W, W symmetric), F = T^T Omega, A = F + H
+        if (b.compact)
+            AJ_TRY(csc_compact_tw<double>(b.cs, S, p->w_compact, p->N, p->native_index, M, b.TW, info, st));
+        else
+            AJ_TRY(csc_spmm_t<double, double>(b.cs, S, p->w_tilde64, M, M, b.TW, M, st));
+        AJ_TRY(transpose<double>(b.TW, S, M, b.Om, st));
+        AJ_TRY(csc_spmm_t<double, double>(b.cs, S, b.Om, S, S, b.F, S, st));
+        add_kernel<<<blocks_for(S * S, 256, 8 * num_sms()), 256, 0, st>>>(b.F, b.H, b.A, S * S);
+        AJ_LAUNCHED();
+        AJ_TRY(spd_factor(b.A, S, b.wa, b.logdets + 0, info, st));
+        AJ_TRY(spd_factor(b.H, S, b.wh, b.logdets + 1, info, st));
+        AJ_TRY(spd_solve_vec(S, b.wa, b.D, b.s, info, st));
+    } else {
+        // the same chain in double-float on the float32 pipe
+        const float *Wh = p->w_tilde_hi, *Wl = p->w_tilde_lo;
+        if (b.compact) {
+            AJ_TRY(csc_compact_tw<double>(b.cs, S, p->w_compact, p->N, p->native_index, M, b.TW, info, st));
+            AJ_TRY(df_split(b.TW, S * M, b.TWh, b.TWl, st));
+        } else {
+            if (!Wh || !Wl) {
+                AJ_TRY(df_split(p->w_tilde64, M * M, b.Wh, b.Wl, st));
+                Wh = b.Wh;
+                Wl = b.Wl;
+            }
+            AJ_TRY(csc_spmm_t_df(b.cs, S, Wh, Wl, M, M, b.TWh, b.TWl, M, st));
+        }
+        AJ_TRY(transpose<float>(b.TWh, S, M, b.Omh, st));
+        AJ_TRY(transpose<float>(b.TWl, S, M, b.Oml, st));
+        AJ_TRY(csc_spmm_t_df(b.cs, S, b.Omh, b.Oml, S, S, b.Fh, b.Fl, S, st));
+        AJ_TRY(df_add_f64(b.Fh, b.Fl, b.H, S * S, b.Ah, b.Al, st));
+        laplacian_shift_kernel<<<1, 1024, 0, st>>>(p->neighbors, p->neighbors_sizes, S, p->P, p->coefficient,
+                                                   p->coefficient_dev, b.logdets + 4);
+        AJ_LAUNCHED();
+        split_shifted_kernel<<<blocks_for(S * S, 256, 8 * num_sms()), 256, 0, st>>>(b.H, S, b.logdets + 4, b.Hh, b.Hl);
+        AJ_LAUNCHED();
+        AJ_TRY(dfspd_factor(b.Ah, b.Al, S, b.da, b.logdets + 0, info, st));
+        AJ_TRY(dfspd_factor(b.Hh, b.Hl, S, b.dh, b.logdets + 1, info, st));
+        AJ_TRY(dfspd_invert_factor(S, b.da, st));
+        AJ_TRY(dfspd_solve_refined(S, b.da, b.Ah, b.Al, b.D, b.s, b.res, st));
+    }
 
     // chi.chi and sum log|noise| over the 2K reals, then logE
     if (K > 0) {
@@ -314,7 +454,8 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
     } else if (cudaMemsetAsync(b.kpart, 0, sizeof(double) * 2 * b.nk_blocks, st) != cudaSuccess) {
         return AJ_ERR_CUDA;
     }
-    assemble_kernel<<<1, 1024, 0, st>>>(b.kpart, b.nk_blocks, K, b.s, b.D, S, b.logdets, out);
+    assemble_kernel<<<1, 1024, 0, st>>>(b.kpart, b.nk_blocks, K, b.s, b.D, S, b.logdets, mixed ? b.logdets + 4 : nullptr,
+                                        out);
     AJ_LAUNCHED();
     if (reconstruction &&
         cudaMemcpyAsync(reconstruction, b.s, sizeof(double) * S, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
@@ -322,13 +463,21 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
     if (!with_grad) return AJ_OK;
 
     // adjoint
-    AJ_TRY(spd_invert_factor(S, b.wa, info, st));
-    AJ_TRY(spd_inverse_from_factor(S, b.wa, b.Ainv, st));
-    AJ_TRY(spd_invert_factor(S, b.wh, info, st));
-    frob_lower_kernel<<<(unsigned)b.nfrob, 256, 0, st>>>(b.wh.Linv, S, b.fpart);
-    AJ_LAUNCHED();
+    if (!mixed) {
+        AJ_TRY(spd_invert_factor(S, b.wa, info, st));
+        AJ_TRY(spd_inverse_from_factor(S, b.wa, b.Ainv, st));
+        AJ_TRY(spd_invert_factor(S, b.wh, info, st));
+        frob_lower_kernel<<<(unsigned)b.nfrob, 256, 0, st>>>(b.wh.Linv, S, b.fpart);
+        AJ_LAUNCHED();
+    } else {
+        AJ_TRY(dfspd_inverse_from_factor(S, b.da, b.AIh, b.AIl, st));
+        AJ_TRY(df_join(b.AIh, b.AIl, S * S, b.Ainv, st));
+        AJ_TRY(df_join(b.Omh, b.Oml, M * S, b.Om, st));
+        AJ_TRY(dfspd_invert_factor(S, b.dh, st));
+        AJ_TRY(df_frob_lower(b.dh.Ih, b.dh.Il, S, b.fpart, b.nfrob, st));
+    }
     dlam_kernel<<<1, 1024, 0, st>>>(p->neighbors, p->neighbors_sizes, S, p->P, b.s, b.Ainv, b.fpart, b.nfrob,
-                                    p->coefficient, p->coefficient_dev, out);
+                                    p->coefficient, p->coefficient_dev, mixed ? b.logdets + 4 : nullptr, out);
     AJ_LAUNCHED();
     if (M > 0 && B > 0) {
         weight_grad_kernel<<<blocks_for(M * 32, 256), 256, 0, st>>>(p->pix_indexes, M, B, S, b.Om, b.Ainv, b.s,

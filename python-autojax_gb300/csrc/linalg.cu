@@ -154,10 +154,15 @@ template int transpose<float>(const float*, int64_t, int64_t, float*, cudaStream
 // -------------------------------------------------------------- Cholesky
 
 // Factor the diagonal block at k0 in place and store its inverse in dinv (NB x NB, lower).
+// One barrier a column: every thread evaluates the pivot (rsqrt) itself and the
+// scaled column goes to a separate array, so the rank-1 update can read the
+// unscaled one; the inverse splits each column's substitution over 8 threads.
 __global__ void __launch_bounds__(256)
     chol_diag_kernel(double* __restrict__ L, int64_t S, int64_t k0, double* __restrict__ dinv, int* info) {
     __shared__ double a[NB][NB + 1];
+    __shared__ double l[NB][NB + 1];
     __shared__ double inv[NB][NB + 1];
+    __shared__ double rinv[NB];
     __shared__ int bad;
     const int tid = threadIdx.x;
     const int64_t nb = (S - k0) < NB ? (S - k0) : NB;
@@ -170,47 +175,50 @@ __global__ void __launch_bounds__(256)
         else
             v = (i == j) ? 1.0 : 0.0;  // identity padding past the matrix end
         a[i][j] = v;
+        l[i][j] = 0.0;
+        inv[i][j] = 0.0;
     }
-    __syncthreads();
+    const int ur = tid >> 3, uq = tid & 7;
     for (int j = 0; j < NB; ++j) {
-        if (tid == 0) {
-            const double d = a[j][j];
-            if (!(d > 0.0)) {
+        __syncthreads();
+        const double d = a[j][j];
+        if (!(d > 0.0)) {
+            if (tid == 0) {
                 bad = 1;
                 report(info, AJ_INFO_NOT_POSITIVE_DEFINITE, k0 + j);
             }
-            a[j][j] = sqrt(d);
+            break;
         }
-        __syncthreads();
-        if (bad) break;
-        if (tid > j && tid < NB) a[tid][j] /= a[j][j];
-        __syncthreads();
-        {
-            const int r = tid >> 3, q = tid & 7;
-            if (r > j) {
+        const double r = rsqrt(d);
+        if (tid == 0) {
+            l[j][j] = d * r;
+            rinv[j] = r;
+        }
+        if (ur > j) {
+            const double lrj = a[ur][j] * r;
+            if (uq == 0) l[ur][j] = lrj;
 #pragma unroll
-                for (int c = q; c < NB; c += 8)
-                    if (c > j && c <= r) a[r][c] = fma(-a[r][j], a[c][j], a[r][c]);
-            }
-        }
-        __syncthreads();
-    }
-    if (bad) return;
-    // inverse of the lower-triangular factor, one column per thread of warp 0
-    if (tid < NB) {
-        const int c = tid;
-        for (int i = 0; i < NB; ++i) inv[i][c] = 0.0;
-        inv[c][c] = 1.0 / a[c][c];
-        for (int i = c + 1; i < NB; ++i) {
-            double s = 0.0;
-            for (int p = c; p < i; ++p) s = fma(a[i][p], inv[p][c], s);
-            inv[i][c] = -s / a[i][i];
+            for (int c = uq; c < NB; c += 8)
+                if (c > j && c <= ur) a[ur][c] = fma(-lrj, a[c][j] * r, a[ur][c]);
         }
     }
     __syncthreads();
+    if (bad) return;
+    const int c = tid >> 3, q = tid & 7;
+    if (tid < NB) inv[tid][tid] = rinv[tid];
+    __syncthreads();
+    for (int i = 1; i < NB; ++i) {
+        double part = 0.0;
+        if (c < i)
+            for (int p = c + q; p < i; p += 8) part = fma(l[i][p], inv[p][c], part);
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+        if (c < i && q == 0) inv[i][c] = -part * rinv[i];
+        __syncthreads();
+    }
     for (int e = tid; e < NB * NB; e += 256) {
         const int i = e / NB, j = e % NB;
-        if (i < nb && j < nb) L[(k0 + i) * S + k0 + j] = (j <= i) ? a[i][j] : 0.0;
+        if (i < nb && j < nb) L[(k0 + i) * S + k0 + j] = (j <= i) ? l[i][j] : 0.0;
         dinv[e] = inv[i][j];
     }
 }
@@ -523,6 +531,22 @@ int aj_spd_logdet(const double* A, int64_t S, double* out, void* workspace, size
     Carver cv(workspace, workspace_bytes);
     SpdWorkspace w = spd_carve(cv, S, false);
     return spd_factor(A, S, w, out, info, st);
+}
+
+size_t aj_spd_inverse_workspace_size(int64_t S) { return spd_workspace_bytes(S, true); }
+
+int aj_spd_inverse(const double* A, int64_t S, double* Ainv, double* logdet, void* workspace, size_t workspace_bytes,
+                   int* info, void* stream) {
+    if (S < 0) return AJ_ERR_ARG;
+    if (S == 0) return AJ_OK;
+    if (!A || !Ainv) return AJ_ERR_ARG;
+    if (!workspace || workspace_bytes < spd_workspace_bytes(S, true)) return AJ_ERR_WORKSPACE;
+    cudaStream_t st = as_stream(stream);
+    Carver cv(workspace, workspace_bytes);
+    SpdWorkspace w = spd_carve(cv, S, true);
+    AJ_TRY(spd_factor(A, S, w, logdet, info, st));
+    AJ_TRY(spd_invert_factor(S, w, info, st));
+    return spd_inverse_from_factor(S, w, Ainv, st);
 }
 
 }  // extern "C"

@@ -1,0 +1,758 @@
+// Double-float (float32 hi + lo) linear algebra for the mixed-precision path.
+//
+// GB300 issues ~62x more float32 than float64 operations per clock, so the
+// S^3 work of the evaluation (two Cholesky factorisations, two triangular
+// inverses, A^-1 = L^-T L^-1) runs as double-float on the float32 pipe:
+// ~15 float32 operations per multiply-add with ~2^-47 relative rounding
+// (float64 keeps 2^-53; the inversion's conditioning needs better than
+// float32's 2^-24, see the mixed-precision notes in the design document).
+//
+// Matrices are row-major S x S with separate hi and lo float planes.
+// Blocked algorithms use NB = 32; the diagonal block of every step is
+// factored (and inverted) redundantly by every block of the panel kernel, so
+// one launch per step both factors the pivot block and solves the rows below.
+
+#include <math.h>
+
+#include "aj_internal.cuh"
+#include "df32.cuh"
+
+namespace aj {
+
+constexpr int DNB = 32;
+
+__device__ __forceinline__ df dfmul(df a, df b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return df_norm({p, e});
+}
+
+__device__ __forceinline__ df dfsqrt(df d) {
+    const float y = sqrtf(d.hi);
+    if (!(y > 0.f)) return {y, 0.f};
+    const float p = y * y;
+    const float e = fmaf(y, y, -p);
+    const float diff = ((d.hi - p) - e) + d.lo;
+    return df_norm({y, diff * (0.5f / y)});
+}
+
+__device__ __forceinline__ df dfrcp(df l) {
+    const float r0 = 1.0f / l.hi;
+    const float q = l.hi * r0;
+    const float qe = fmaf(l.hi, r0, -q) + l.lo * r0;
+    const float one_minus = (1.0f - q) - qe;
+    return df_norm({r0, r0 * one_minus});
+}
+
+// 1/sqrt(d) to double-float accuracy: hardware rsqrt, one float Newton step,
+// one double-float Newton step (no divisions on the critical path)
+__device__ __forceinline__ df dfrsqrt(df d) {
+    float r = rsqrtf(d.hi);
+    r = r * fmaf(-0.5f * d.hi * r, r, 1.5f);
+    const float q = r * r;
+    const float qe = fmaf(r, r, -q);
+    const df t = dfmul(d, {q, qe});
+    const float h = (1.0f - t.hi) - t.lo;
+    return df_norm({r, 0.5f * r * h});
+}
+
+__device__ __forceinline__ void lower_tile_df(int64_t t, int64_t& bi, int64_t& bj) {
+    int64_t r = static_cast<int64_t>((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (r * (r + 1) / 2 > t) --r;
+    while ((r + 1) * (r + 2) / 2 <= t) ++r;
+    bi = r;
+    bj = t - r * (r + 1) / 2;
+}
+
+// ----------------------------------------------------------------- planes
+
+__global__ void split_kernel(const double* __restrict__ x, int64_t n, float* __restrict__ hi, float* __restrict__ lo) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const df v = df_from(x[t]);
+        hi[t] = v.hi;
+        lo[t] = v.lo;
+    }
+}
+
+__global__ void join_kernel(const float* __restrict__ hi, const float* __restrict__ lo, int64_t n,
+                            double* __restrict__ x) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        x[t] = (double)hi[t] + (double)lo[t];
+}
+
+// (hi, lo) = df(a) + df(b) for float64 a (plane pair given) and double b
+__global__ void add_df_f64_kernel(const float* __restrict__ ah, const float* __restrict__ al,
+                                  const double* __restrict__ b, int64_t n, float* __restrict__ oh,
+                                  float* __restrict__ ol) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const df v = df_add({ah[t], al[t]}, df_from(b[t]));
+        oh[t] = v.hi;
+        ol[t] = v.lo;
+    }
+}
+
+// ------------------------------------------------------------------- GEMM
+
+// C (m x n) = (neg ? -1 : 1) op(A) op(B) (+ C when accumulate), double-float planes.
+// 64 x 64 tiles, 256 threads with 4 x 4 accumulators each; the k loop runs in
+// 32-deep slabs staged through shared memory with the next slab prefetched
+// into registers, products accumulate lazily (renormalised every 8 k).
+constexpr int GBK = 32;
+
+template <bool TA, bool TB>
+__device__ __forceinline__ void gemm_df_load(const float* __restrict__ Ah, const float* __restrict__ Al, int64_t lda,
+                                             const float* __restrict__ Bh, const float* __restrict__ Bl, int64_t ldb,
+                                             int64_t m, int64_t n, int64_t k, int64_t i0, int64_t j0, int64_t k0,
+                                             int tid, float (&ra)[16], float (&rb)[16]) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int e = tid + q * 256;  // 2048 = 64 x 32 elements per operand slab
+        int ii, kk;
+        if (TA) {
+            kk = e >> 6;
+            ii = e & 63;
+        } else {
+            ii = e >> 5;
+            kk = e & 31;
+        }
+        const int64_t gi = i0 + ii, gk = k0 + kk;
+        float vh = 0.f, vl = 0.f;
+        if (gi < m && gk < k) {
+            const int64_t off = TA ? gk * lda + gi : gi * lda + gk;
+            vh = Ah[off];
+            vl = Al[off];
+        }
+        ra[2 * q] = vh;
+        ra[2 * q + 1] = vl;
+        int jj, kb;
+        if (TB) {
+            jj = e >> 5;
+            kb = e & 31;
+        } else {
+            kb = e >> 6;
+            jj = e & 63;
+        }
+        const int64_t gj = j0 + jj, gk2 = k0 + kb;
+        float wh = 0.f, wl = 0.f;
+        if (gj < n && gk2 < k) {
+            const int64_t off = TB ? gj * ldb + gk2 : gk2 * ldb + gj;
+            wh = Bh[off];
+            wl = Bl[off];
+        }
+        rb[2 * q] = wh;
+        rb[2 * q + 1] = wl;
+    }
+}
+
+template <bool TA, bool TB>
+__device__ __forceinline__ void gemm_df_store(float (*sAh)[68], float (*sAl)[68], float (*sBh)[68], float (*sBl)[68],
+                                              int tid, const float (&ra)[16], const float (&rb)[16]) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int e = tid + q * 256;
+        int ii, kk, jj, kb;
+        if (TA) {
+            kk = e >> 6;
+            ii = e & 63;
+        } else {
+            ii = e >> 5;
+            kk = e & 31;
+        }
+        if (TB) {
+            jj = e >> 5;
+            kb = e & 31;
+        } else {
+            kb = e >> 6;
+            jj = e & 63;
+        }
+        sAh[kk][ii] = ra[2 * q];
+        sAl[kk][ii] = ra[2 * q + 1];
+        sBh[kb][jj] = rb[2 * q];
+        sBl[kb][jj] = rb[2 * q + 1];
+    }
+}
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256)
+    gemm_df_kernel(int64_t m, int64_t n, int64_t k, int neg, const float* __restrict__ Ah, const float* __restrict__ Al,
+                   int64_t lda, const float* __restrict__ Bh, const float* __restrict__ Bl, int64_t ldb, int accumulate,
+                   float* __restrict__ Ch, float* __restrict__ Cl, int64_t ldc, int lower_only, int tri_k,
+                   int64_t tiles_n) {
+    __shared__ float sAh[GBK][68], sAl[GBK][68], sBh[GBK][68], sBl[GBK][68];
+    int64_t ti, tj;
+    if (lower_only)
+        lower_tile_df(blockIdx.x, ti, tj);
+    else {
+        ti = blockIdx.x / tiles_n;
+        tj = blockIdx.x % tiles_n;
+    }
+    const int64_t i0 = ti * 64, j0 = tj * 64;
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    df acc[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = {0.f, 0.f};
+    const int64_t kbeg = tri_k ? (i0 > j0 ? i0 : j0) : 0;
+    float ra[16], rb[16];
+    if (kbeg < k) gemm_df_load<TA, TB>(Ah, Al, lda, Bh, Bl, ldb, m, n, k, i0, j0, kbeg, tid, ra, rb);
+    for (int64_t k0 = kbeg; k0 < k; k0 += GBK) {
+        gemm_df_store<TA, TB>(sAh, sAl, sBh, sBl, tid, ra, rb);
+        __syncthreads();
+        if (k0 + GBK < k) gemm_df_load<TA, TB>(Ah, Al, lda, Bh, Bl, ldb, m, n, k, i0, j0, k0 + GBK, tid, ra, rb);
+#pragma unroll
+        for (int k8 = 0; k8 < GBK; k8 += 8) {
+#pragma unroll
+            for (int kk = k8; kk < k8 + 8; ++kk) {
+                df a[4], b[4];
+#pragma unroll
+                for (int r = 0; r < 4; ++r) a[r] = {sAh[kk][ty * 4 + r], sAl[kk][ty * 4 + r]};
+#pragma unroll
+                for (int c = 0; c < 4; ++c) b[c] = {sBh[kk][tx * 4 + c], sBl[kk][tx * 4 + c]};
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) df_fma_lazy(acc[r][c], a[r], b[c]);
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) df_renorm(acc[r][c]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int64_t gi = i0 + ty * 4 + r, gj = j0 + tx * 4 + c;
+            if (gi < m && gj < n) {
+                df v = neg ? df_neg(acc[r][c]) : acc[r][c];
+                if (accumulate) v = df_add(v, {Ch[gi * ldc + gj], Cl[gi * ldc + gj]});
+                Ch[gi * ldc + gj] = v.hi;
+                Cl[gi * ldc + gj] = v.lo;
+            }
+        }
+}
+
+int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const float* Ah, const float* Al, int64_t lda,
+            const float* Bh, const float* Bl, int64_t ldb, bool accumulate, float* Ch, float* Cl, int64_t ldc,
+            bool lower_only, bool tri_k, cudaStream_t st) {
+    if (m <= 0 || n <= 0) return AJ_OK;
+    const int64_t tm = (m + 63) / 64, tn = (n + 63) / 64;
+    const unsigned g = (unsigned)(lower_only ? tm * (tm + 1) / 2 : tm * tn);
+#define AJ_DF_GEMM(a, b)                                                                                          \
+    gemm_df_kernel<a, b><<<g, 256, 0, st>>>(m, n, k, neg ? 1 : 0, Ah, Al, lda, Bh, Bl, ldb, accumulate ? 1 : 0, Ch, \
+                                            Cl, ldc, lower_only ? 1 : 0, tri_k ? 1 : 0, tn)
+    if (!ta && !tb)
+        AJ_DF_GEMM(false, false);
+    else if (!ta && tb)
+        AJ_DF_GEMM(false, true);
+    else if (ta && !tb)
+        AJ_DF_GEMM(true, false);
+    else
+        AJ_DF_GEMM(true, true);
+#undef AJ_DF_GEMM
+    return check_launch();
+}
+
+// -------------------------------------------------------------- Cholesky
+
+// Factor + invert the diagonal block at k0 (every block, redundantly), then:
+// block 0 stores L_kk, its inverse and the pivots; block b >= 1 replaces the
+// 64 panel rows k0 + 32 + 64 (b - 1) .. by A_rows L_kk^-T.
+// Latency matters more than work here (one launch per 32 columns sits on the
+// critical path): the pivot step fuses the column scaling into the rank-1
+// update (two barriers a column), and the inverse spreads each column's
+// substitution over 8 threads whose partial dot products meet in shuffles.
+__global__ void __launch_bounds__(256)
+    dfchol_panel_kernel(float* __restrict__ Lh, float* __restrict__ Ll, int64_t S, int64_t k0,
+                        float* __restrict__ dh, float* __restrict__ dl, double* __restrict__ piv, int* info) {
+    __shared__ float ah[DNB][DNB + 1], al[DNB][DNB + 1];
+    __shared__ float ih[DNB][DNB + 1], il[DNB][DNB + 1];
+    __shared__ float lh[DNB][DNB + 1], ll[DNB][DNB + 1];
+    __shared__ float rh[DNB], rl[DNB];
+    __shared__ float xh[64][DNB + 1], xl[64][DNB + 1];
+    __shared__ int bad;
+    const int tid = threadIdx.x;
+    const int64_t nb = (S - k0) < DNB ? (S - k0) : DNB;
+    if (tid == 0) bad = 0;
+    for (int e = tid; e < DNB * DNB; e += 256) {
+        const int i = e / DNB, j = e % DNB;
+        float vh, vl;
+        if (i < nb && j < nb) {
+            const int64_t off = (k0 + i) * S + k0 + j;
+            vh = j <= i ? Lh[off] : 0.f;
+            vl = j <= i ? Ll[off] : 0.f;
+        } else {
+            vh = i == j ? 1.f : 0.f;
+            vl = 0.f;
+        }
+        ah[i][j] = vh;
+        al[i][j] = vl;
+        ih[i][j] = 0.f;
+        il[i][j] = 0.f;
+        lh[i][j] = 0.f;
+        ll[i][j] = 0.f;
+    }
+    // panel rows are loaded up front so their latency overlaps the factorisation
+    const int64_t r0 = k0 + DNB + (int64_t)(blockIdx.x - 1) * 64;
+    if (blockIdx.x > 0) {
+        for (int e = tid; e < 64 * DNB; e += 256) {
+            const int i = e / DNB, j = e % DNB;
+            const int64_t r = r0 + i;
+            const bool in = r < S && j < nb;
+            xh[i][j] = in ? Lh[r * S + k0 + j] : 0.f;
+            xl[i][j] = in ? Ll[r * S + k0 + j] : 0.f;
+        }
+    }
+    __syncthreads();
+    const int ur = tid >> 3, uq = tid & 7;  // update: row ur, columns uq, uq+8, ...
+    // one barrier a column: every thread evaluates the pivot itself; the scaled
+    // column goes to L (lh/ll) so the update can keep reading the unscaled one
+    for (int j = 0; j < DNB; ++j) {
+        __syncthreads();
+        const df d = {ah[j][j], al[j][j]};
+        if (!(d.hi > 0.f)) {
+            if (tid == 0) {
+                bad = 1;
+                if (blockIdx.x == 0) report(info, AJ_INFO_NOT_POSITIVE_DEFINITE, k0 + j);
+            }
+            break;
+        }
+        const df rj = dfrsqrt(d);
+        if (tid == 0) {
+            const df l = dfmul(d, rj);
+            lh[j][j] = l.hi;
+            ll[j][j] = l.lo;
+            rh[j] = rj.hi;
+            rl[j] = rj.lo;
+            if (blockIdx.x == 0 && j < nb) piv[k0 + j] = df_to(l);
+        }
+        if (ur > j) {
+            const df lrj = dfmul({ah[ur][j], al[ur][j]}, rj);
+            if (uq == 0) {
+                lh[ur][j] = lrj.hi;
+                ll[ur][j] = lrj.lo;
+            }
+#pragma unroll
+            for (int c = uq; c < DNB; c += 8)
+                if (c > j && c <= ur) {
+                    const df lcj = dfmul({ah[c][j], al[c][j]}, rj);
+                    df v = {ah[ur][c], al[ur][c]};
+                    df_fms_acc(v, lrj, lcj);
+                    ah[ur][c] = v.hi;
+                    al[ur][c] = v.lo;
+                }
+        }
+    }
+    __syncthreads();
+    if (bad) return;
+    // inverse X = L^-1, row by row: X[i][c] = -r_i sum_{p=c}^{i-1} L[i][p] X[p][c]; thread (c, q)
+    // sums p = c + q, c + q + 8, ... and the 8 partials of a column meet in shuffles
+    const int c = tid >> 3, q = tid & 7;
+    if (tid < DNB) {
+        ih[tid][tid] = rh[tid];
+        il[tid][tid] = rl[tid];
+    }
+    __syncthreads();
+    for (int i = 1; i < DNB; ++i) {
+        df part = {0.f, 0.f};
+        if (c < i)
+            for (int p = c + q; p < i; p += 8) df_fma_acc(part, {lh[i][p], ll[i][p]}, {ih[p][c], il[p][c]});
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {
+            const df other = {__shfl_xor_sync(0xffffffffu, part.hi, o), __shfl_xor_sync(0xffffffffu, part.lo, o)};
+            part = df_add(part, other);
+        }
+        if (c < i && q == 0) {
+            const df v = df_neg(dfmul(part, {rh[i], rl[i]}));
+            ih[i][c] = v.hi;
+            il[i][c] = v.lo;
+        }
+        __syncthreads();
+    }
+    if (blockIdx.x == 0) {
+        for (int e = tid; e < DNB * DNB; e += 256) {
+            const int i = e / DNB, j = e % DNB;
+            if (i < nb && j < nb) {
+                const int64_t off = (k0 + i) * S + k0 + j;
+                Lh[off] = j <= i ? lh[i][j] : 0.f;
+                Ll[off] = j <= i ? ll[i][j] : 0.f;
+            }
+            dh[e] = ih[i][j];
+            dl[e] = il[i][j];
+        }
+        return;
+    }
+    const int i = tid >> 2, qq = tid & 3;  // 64 rows x 4 column groups of 8
+    df out[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) out[t] = {0.f, 0.f};
+    for (int p = 0; p < DNB; ++p) {
+        const df x = {xh[i][p], xl[i][p]};
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int cc = qq + 4 * t;
+            if (p <= cc) df_fma_acc(out[t], x, {ih[cc][p], il[cc][p]});
+        }
+    }
+    const int64_t r = r0 + i;
+    if (r < S)
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int cc = qq + 4 * t;
+            if (cc < nb) {
+                Lh[r * S + k0 + cc] = out[t].hi;
+                Ll[r * S + k0 + cc] = out[t].lo;
+            }
+        }
+}
+
+// Trailing update of one Cholesky step: C (lower 32 x 32 tiles of the r x r
+// trailing matrix) -= P P^T with P the r x 32 solved panel.  128 threads, 8
+// outputs each; small register and shared footprint so several blocks share
+// an SM and the late, small steps still fill the GPU.
+__global__ void __launch_bounds__(128)
+    dfsyrk_update_kernel(float* __restrict__ Lh, float* __restrict__ Ll, int64_t S, int64_t k0) {
+    __shared__ float pih[32][33], pil[32][33], pjh[32][33], pjl[32][33];
+    const int64_t r0 = k0 + DNB;
+    int64_t ti, tj;
+    lower_tile_df(blockIdx.x, ti, tj);
+    const int64_t i0 = r0 + ti * 32, j0 = r0 + tj * 32;
+    const int tid = threadIdx.x;
+    for (int e = tid; e < 32 * 32; e += 128) {
+        const int a = e >> 5, b = e & 31;
+        const bool ii = i0 + a < S, jj = j0 + a < S;
+        pih[a][b] = ii ? Lh[(i0 + a) * S + k0 + b] : 0.f;
+        pil[a][b] = ii ? Ll[(i0 + a) * S + k0 + b] : 0.f;
+        pjh[a][b] = jj ? Lh[(j0 + a) * S + k0 + b] : 0.f;
+        pjl[a][b] = jj ? Ll[(j0 + a) * S + k0 + b] : 0.f;
+    }
+    __syncthreads();
+    const int ty = tid >> 3, tx = tid & 7;  // rows ty, ty+16; columns tx, tx+8, tx+16, tx+24
+    df acc[2][4];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = {0.f, 0.f};
+#pragma unroll
+    for (int k8 = 0; k8 < 32; k8 += 8) {
+#pragma unroll
+        for (int k = k8; k < k8 + 8; ++k) {
+            const df x0 = {pih[ty][k], pil[ty][k]}, x1 = {pih[ty + 16][k], pil[ty + 16][k]};
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const df y = {pjh[tx + 8 * b][k], pjl[tx + 8 * b][k]};
+                df_fma_lazy(acc[0][b], x0, y);
+                df_fma_lazy(acc[1][b], x1, y);
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) df_renorm(acc[a][b]);
+    }
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int64_t gi = i0 + ty + 16 * a, gj = j0 + tx + 8 * b;
+            if (gi < S && gj < S && gj <= gi) {
+                const df v = df_add({Lh[gi * S + gj], Ll[gi * S + gj]}, df_neg(acc[a][b]));
+                Lh[gi * S + gj] = v.hi;
+                Ll[gi * S + gj] = v.lo;
+            }
+        }
+}
+
+__global__ void df_zero_upper_kernel(float* __restrict__ h, float* __restrict__ l, int64_t S) {
+    for (int64_t i = blockIdx.y; i < S; i += gridDim.y)
+        for (int64_t j = i + 1 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < S;
+             j += (int64_t)gridDim.x * blockDim.x) {
+            h[i * S + j] = 0.f;
+            l[i * S + j] = 0.f;
+        }
+}
+
+__global__ void df_logdet_kernel(const double* __restrict__ piv, int64_t S, double* __restrict__ out,
+                                 const int* info) {
+    __shared__ double red[32];
+    double acc = 0.0;
+    for (int64_t i = threadIdx.x; i < S; i += blockDim.x) acc += log(piv[i]);
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) *out = (info && info[0] == AJ_INFO_NOT_POSITIVE_DEFINITE) ? NAN : 2.0 * acc;
+}
+
+// ---------------------------------------------------- triangular inverse
+
+__global__ void df_linv_init_kernel(float* __restrict__ Ih, float* __restrict__ Il, int64_t S,
+                                    const float* __restrict__ dh, const float* __restrict__ dl) {
+    const int64_t kb = blockIdx.x, k0 = kb * DNB;
+    for (int e = threadIdx.x; e < DNB * DNB; e += blockDim.x) {
+        const int i = e / DNB, j = e % DNB;
+        if (k0 + i < S && k0 + j < S) {
+            Ih[(k0 + i) * S + k0 + j] = dh[kb * DNB * DNB + e];
+            Il[(k0 + i) * S + k0 + j] = dl[kb * DNB * DNB + e];
+        }
+    }
+}
+
+// see trtri_step_kernel (linalg.cu): accumulate L[ti][kb] X[kb][tj]; block row kb + 1 applies -dinv
+__global__ void __launch_bounds__(256)
+    df_trtri_step_kernel(const float* __restrict__ Lh, const float* __restrict__ Ll, float* __restrict__ Ih,
+                         float* __restrict__ Il, int64_t S, int64_t kb, const float* __restrict__ dh,
+                         const float* __restrict__ dl) {
+    __shared__ float ah[32][33], al[32][33], bh[32][33], bl[32][33];
+    const int64_t nbt = (S + DNB - 1) / DNB;
+    const int64_t ncol = kb + 1;
+    const int64_t ti = kb + 1 + blockIdx.x / ncol, tj = blockIdx.x % ncol;
+    if (ti >= nbt) return;
+    const int tid = threadIdx.x;
+    const int64_t i0 = ti * DNB, j0 = tj * DNB, p0 = kb * DNB;
+    for (int e = tid; e < DNB * DNB; e += 256) {
+        const int r = e / DNB, c = e % DNB;
+        const bool ina = i0 + r < S && p0 + c < S, inb = p0 + r < S && j0 + c < S;
+        ah[r][c] = ina ? Lh[(i0 + r) * S + p0 + c] : 0.f;
+        al[r][c] = ina ? Ll[(i0 + r) * S + p0 + c] : 0.f;
+        bh[r][c] = inb ? Ih[(p0 + r) * S + j0 + c] : 0.f;
+        bl[r][c] = inb ? Il[(p0 + r) * S + j0 + c] : 0.f;
+    }
+    __syncthreads();
+    const int r = tid >> 3, q = tid & 7;
+    df acc[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        const int c = q + 8 * t;
+        const bool in = i0 + r < S && j0 + c < S;
+        df s = in ? df{Ih[(i0 + r) * S + j0 + c], Il[(i0 + r) * S + j0 + c]} : df{0.f, 0.f};
+        for (int p = 0; p < DNB; ++p) df_fma_acc(s, {ah[r][p], al[r][p]}, {bh[p][c], bl[p][c]});
+        acc[t] = s;
+    }
+    if (ti != kb + 1) {
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int c = q + 8 * t;
+            if (i0 + r < S && j0 + c < S) {
+                Ih[(i0 + r) * S + j0 + c] = acc[t].hi;
+                Il[(i0 + r) * S + j0 + c] = acc[t].lo;
+            }
+        }
+        return;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        ah[r][q + 8 * t] = acc[t].hi;
+        al[r][q + 8 * t] = acc[t].lo;
+    }
+    for (int e = tid; e < DNB * DNB; e += 256) {
+        bh[e / DNB][e % DNB] = dh[(kb + 1) * DNB * DNB + e];
+        bl[e / DNB][e % DNB] = dl[(kb + 1) * DNB * DNB + e];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        const int c = q + 8 * t;
+        df s = {0.f, 0.f};
+        for (int p = 0; p <= r; ++p) df_fma_acc(s, {bh[r][p], bl[r][p]}, {ah[p][c], al[p][c]});
+        if (i0 + r < S && j0 + c < S) {
+            Ih[(i0 + r) * S + j0 + c] = -s.hi;
+            Il[(i0 + r) * S + j0 + c] = -s.lo;
+        }
+    }
+}
+
+__global__ void df_mirror_lower_kernel(float* __restrict__ h, float* __restrict__ l, int64_t S) {
+    for (int64_t i = blockIdx.y; i < S; i += gridDim.y)
+        for (int64_t j = i + 1 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < S;
+             j += (int64_t)gridDim.x * blockDim.x) {
+            h[i * S + j] = h[j * S + i];
+            l[i * S + j] = l[j * S + i];
+        }
+}
+
+// y = op(Li) x for lower-triangular Li (double-float), x and y float64; one warp per output
+__global__ void __launch_bounds__(256)
+    df_trmv_kernel(const float* __restrict__ Lh, const float* __restrict__ Ll, int64_t S, int trans,
+                   const double* __restrict__ x, double* __restrict__ y) {
+    const int lane = threadIdx.x & 31;
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (i >= S) return;
+    df acc = {0.f, 0.f};
+    if (!trans) {
+        for (int64_t j = lane; j <= i; j += 32) df_fma_acc(acc, {Lh[i * S + j], Ll[i * S + j]}, df_from(x[j]));
+    } else {
+        for (int64_t j = i + lane; j < S; j += 32) df_fma_acc(acc, {Lh[j * S + i], Ll[j * S + i]}, df_from(x[j]));
+    }
+    double v = df_to(acc);
+    v = warp_sum(v);
+    if (lane == 0) y[i] = v;
+}
+
+// r = b - A x for a full double-float A (x, b, r float64); one warp per row
+__global__ void __launch_bounds__(256)
+    df_residual_kernel(const float* __restrict__ Ah, const float* __restrict__ Al, int64_t S,
+                       const double* __restrict__ x, const double* __restrict__ b, double* __restrict__ r) {
+    const int lane = threadIdx.x & 31;
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (i >= S) return;
+    df acc = {0.f, 0.f};
+    for (int64_t j = lane; j < S; j += 32) df_fma_acc(acc, {Ah[i * S + j], Al[i * S + j]}, df_from(x[j]));
+    double v = df_to(acc);
+    v = warp_sum(v);
+    if (lane == 0) r[i] = b[i] - v;
+}
+
+__global__ void add_vec_kernel(double* __restrict__ x, const double* __restrict__ d, int64_t n) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        x[t] += d[t];
+}
+
+// partial sums of squares of a lower-triangular double-float matrix
+__global__ void df_frob_lower_kernel(const float* __restrict__ h, const float* __restrict__ l, int64_t S,
+                                     double* __restrict__ partial) {
+    __shared__ double red[32];
+    double acc = 0.0;
+    for (int64_t i = blockIdx.x; i < S; i += gridDim.x)
+        for (int64_t j = threadIdx.x; j <= i; j += blockDim.x) {
+            const double v = (double)h[i * S + j] + (double)l[i * S + j];
+            acc = fma(v, v, acc);
+        }
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+}
+
+// ------------------------------------------------------------ host side
+
+size_t dfspd_bytes(int64_t S, bool with_inverse) {
+    const int64_t nbt = (S + DNB - 1) / DNB;
+    Sizer s;
+    s.take<float>(2 * S * S);  // L planes
+    if (with_inverse) s.take<float>(2 * S * S);
+    s.take<float>(2 * nbt * DNB * DNB);
+    s.take<double>(S);  // pivots
+    s.take<double>(S);  // vector scratch
+    return s.total();
+}
+
+DfSpd dfspd_carve(Carver& cv, int64_t S, bool with_inverse) {
+    const int64_t nbt = (S + DNB - 1) / DNB;
+    DfSpd w;
+    float* L = cv.take<float>(2 * S * S);
+    w.Lh = L;
+    w.Ll = L ? L + S * S : nullptr;
+    if (with_inverse) {
+        float* I = cv.take<float>(2 * S * S);
+        w.Ih = I;
+        w.Il = I ? I + S * S : nullptr;
+    } else {
+        w.Ih = w.Il = nullptr;
+    }
+    float* d = cv.take<float>(2 * nbt * DNB * DNB);
+    w.dh = d;
+    w.dl = d ? d + nbt * DNB * DNB : nullptr;
+    w.piv = cv.take<double>(S);
+    w.vec = cv.take<double>(S);
+    return w;
+}
+
+int df_split(const double* x, int64_t n, float* hi, float* lo, cudaStream_t st) {
+    split_kernel<<<blocks_for(n, 256, 8 * num_sms()), 256, 0, st>>>(x, n, hi, lo);
+    return check_launch();
+}
+
+int df_join(const float* hi, const float* lo, int64_t n, double* x, cudaStream_t st) {
+    join_kernel<<<blocks_for(n, 256, 8 * num_sms()), 256, 0, st>>>(hi, lo, n, x);
+    return check_launch();
+}
+
+int df_add_f64(const float* ah, const float* al, const double* b, int64_t n, float* oh, float* ol, cudaStream_t st) {
+    add_df_f64_kernel<<<blocks_for(n, 256, 8 * num_sms()), 256, 0, st>>>(ah, al, b, n, oh, ol);
+    return check_launch();
+}
+
+// L (in w) = chol(A); A given as planes (copied unless it is w's own L)
+int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* logdet, int* info, cudaStream_t st) {
+    if (S <= 0) return AJ_OK;
+    if (Ah != w.Lh) {
+        if (cudaMemcpyAsync(w.Lh, Ah, sizeof(float) * S * S, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+            cudaMemcpyAsync(w.Ll, Al, sizeof(float) * S * S, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+            return AJ_ERR_CUDA;
+    }
+    const int64_t nbt = (S + DNB - 1) / DNB;
+    for (int64_t kb = 0; kb < nbt; ++kb) {
+        const int64_t k0 = kb * DNB;
+        const int64_t below = S - k0 - DNB;
+        const unsigned g = 1 + (unsigned)(below > 0 ? (below + 63) / 64 : 0);
+        dfchol_panel_kernel<<<g, 256, 0, st>>>(w.Lh, w.Ll, S, k0, w.dh + kb * DNB * DNB, w.dl + kb * DNB * DNB, w.piv,
+                                               info);
+        AJ_LAUNCHED();
+        if (below > 0) {
+            const int64_t tb = (below + 31) / 32;
+            dfsyrk_update_kernel<<<(unsigned)(tb * (tb + 1) / 2), 128, 0, st>>>(w.Lh, w.Ll, S, k0);
+            AJ_LAUNCHED();
+        }
+    }
+    dim3 zg(blocks_for(S, 256, 8), (unsigned)(S < 65535 ? S : 65535));
+    df_zero_upper_kernel<<<zg, 256, 0, st>>>(w.Lh, w.Ll, S);
+    AJ_LAUNCHED();
+    if (logdet) {
+        df_logdet_kernel<<<1, 1024, 0, st>>>(w.piv, S, logdet, info);
+        AJ_LAUNCHED();
+    }
+    return AJ_OK;
+}
+
+int dfspd_invert_factor(int64_t S, DfSpd& w, cudaStream_t st) {
+    if (S <= 0) return AJ_OK;
+    if (!w.Ih) return AJ_ERR_ARG;
+    const int64_t nbt = (S + DNB - 1) / DNB;
+    if (cudaMemsetAsync(w.Ih, 0, sizeof(float) * 2 * S * S, st) != cudaSuccess) return AJ_ERR_CUDA;
+    df_linv_init_kernel<<<(unsigned)nbt, 256, 0, st>>>(w.Ih, w.Il, S, w.dh, w.dl);
+    AJ_LAUNCHED();
+    for (int64_t kb = 0; kb + 1 < nbt; ++kb) {
+        const int64_t tiles = (nbt - kb - 1) * (kb + 1);
+        df_trtri_step_kernel<<<(unsigned)tiles, 256, 0, st>>>(w.Lh, w.Ll, w.Ih, w.Il, S, kb, w.dh, w.dl);
+        AJ_LAUNCHED();
+    }
+    return AJ_OK;
+}
+
+int dfspd_inverse_from_factor(int64_t S, DfSpd& w, float* Ah, float* Al, cudaStream_t st) {
+    AJ_TRY(gemm_df(true, false, S, S, S, false, w.Ih, w.Il, S, w.Ih, w.Il, S, false, Ah, Al, S, true, true, st));
+    dim3 g(blocks_for(S, 256, 8), (unsigned)(S < 65535 ? S : 65535));
+    df_mirror_lower_kernel<<<g, 256, 0, st>>>(Ah, Al, S);
+    return check_launch();
+}
+
+// x = A^-1 b = Li^T (Li b) with the inverse factor
+int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st) {
+    if (!w.Ih) return AJ_ERR_ARG;
+    const unsigned g = blocks_for(S * 32, 256);
+    df_trmv_kernel<<<g, 256, 0, st>>>(w.Ih, w.Il, S, 0, b, w.vec);
+    AJ_LAUNCHED();
+    df_trmv_kernel<<<g, 256, 0, st>>>(w.Ih, w.Il, S, 1, w.vec, x);
+    return check_launch();
+}
+
+// x = A^-1 b with one step of iterative refinement against A (planes); r is S scratch
+int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x, double* r,
+                        cudaStream_t st) {
+    AJ_TRY(dfspd_solve_vec(S, w, b, x, st));
+    const unsigned g = blocks_for(S * 32, 256);
+    df_residual_kernel<<<g, 256, 0, st>>>(Ah, Al, S, x, b, r);
+    AJ_LAUNCHED();
+    AJ_TRY(dfspd_solve_vec(S, w, r, r, st));
+    add_vec_kernel<<<blocks_for(S, 256, 64), 256, 0, st>>>(x, r, S);
+    return check_launch();
+}
+
+int df_frob_lower(const float* h, const float* l, int64_t S, double* partial, int64_t nparts, cudaStream_t st) {
+    df_frob_lower_kernel<<<(unsigned)nparts, 256, 0, st>>>(h, l, S, partial);
+    return check_launch();
+}
+
+}  // namespace aj

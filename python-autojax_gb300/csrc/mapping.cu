@@ -13,6 +13,7 @@
 //                mapping_matrix_from, numba.py:369-375).
 
 #include "aj_internal.cuh"
+#include "df32.cuh"
 
 namespace aj {
 
@@ -101,83 +102,96 @@ __device__ __forceinline__ bool csc_entry(const int64_t* idx, const int64_t* siz
     return true;
 }
 
-__global__ void csc_count_kernel(const int64_t* __restrict__ idx, const int64_t* __restrict__ sizes, int64_t M,
-                                 int64_t B, int64_t S, CscMode mode, int* __restrict__ count, int* info) {
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < M * B; e += (int64_t)gridDim.x * blockDim.x) {
+// Stable counting sort of the kept entries by source index, entries taken in
+// (m, b) order: chunk c of CSC_CHUNK consecutive entries histograms its
+// columns, a scan over (column, chunk) gives every chunk its write offset in
+// each column, and each chunk then writes its entries in order.  Columns come
+// out sorted by (m, b) — the reference's loop order — with no atomics on the
+// output and no per-column sort, whatever the column lengths.
+constexpr int CSC_CHUNK = 1024;
+
+__global__ void __launch_bounds__(256)
+    csc_hist_kernel(const int64_t* __restrict__ idx, const int64_t* __restrict__ sizes, int64_t M, int64_t B,
+                    int64_t S, CscMode mode, int* __restrict__ hist, int* info) {
+    // hist[chunk][s]
+    const int64_t c = blockIdx.x;
+    const int64_t e0 = c * CSC_CHUNK, e1 = min(M * B, e0 + CSC_CHUNK);
+    int* h = hist + c * S;
+    for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         int64_t s;
-        if (csc_entry(idx, sizes, e / B, e % B, B, S, mode, s, nullptr)) atomicAdd(&count[s], 1);
+        if (csc_entry(idx, sizes, e / B, e % B, B, S, mode, s, info)) atomicAdd(&h[s], 1);
     }
 }
 
-// single block exclusive scan of count[0..S) into colptr[0..S], cursor reset
-__global__ void csc_scan_kernel(int* __restrict__ count, int64_t S, int* __restrict__ colptr) {
+// colptr[s] = sum of all counts of columns < s; off[chunk][s] = colptr[s] + counts of earlier chunks
+__global__ void csc_offsets_kernel(const int* __restrict__ hist, int64_t nchunk, int64_t S, int* __restrict__ colptr,
+                                   int* __restrict__ off) {
     __shared__ int warp_tot[32];
     __shared__ int base;
     if (threadIdx.x == 0) base = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int64_t c0 = 0; c0 < S; c0 += blockDim.x) {
-        const int64_t t = c0 + threadIdx.x;
-        const int v = t < S ? count[t] : 0;
-        int x = v;
+    for (int64_t s0 = 0; s0 < S; s0 += blockDim.x) {
+        const int64_t s = s0 + threadIdx.x;
+        int tot = 0;
+        if (s < S)
+            for (int64_t c = 0; c < nchunk; ++c) tot += hist[c * S + s];
+        int x = tot;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(0xffffffffu, x, o);
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
             if (lane >= o) x += y;
         }
         if (lane == 31) warp_tot[wid] = x;
         __syncthreads();
         int before = 0;
         for (int w = 0; w < wid; ++w) before += warp_tot[w];
-        if (t < S) {
-            colptr[t] = base + before + x - v;
-            count[t] = 0;  // reused as the fill cursor
+        if (s < S) {
+            int run = base + before + x - tot;
+            colptr[s] = run;
+            for (int64_t c = 0; c < nchunk; ++c) {
+                off[c * S + s] = run;
+                run += hist[c * S + s];
+            }
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            int tot = 0;
-            for (int w = 0; w < nw; ++w) tot += warp_tot[w];
-            base += tot;
+            int t = 0;
+            for (int w = 0; w < nw; ++w) t += warp_tot[w];
+            base += t;
         }
         __syncthreads();
     }
     if (threadIdx.x == 0) colptr[S] = base;
 }
 
-__global__ void csc_fill_kernel(const int64_t* __restrict__ idx, const double* __restrict__ w,
-                                const int64_t* __restrict__ sizes, int64_t M, int64_t B, int64_t S, CscMode mode,
-                                const int* __restrict__ colptr, int* __restrict__ cursor, int* __restrict__ rows,
-                                double* __restrict__ vals, int* __restrict__ keys, int* info) {
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < M * B; e += (int64_t)gridDim.x * blockDim.x) {
-        int64_t s;
-        if (csc_entry(idx, sizes, e / B, e % B, B, S, mode, s, info)) {
-            const int pos = colptr[s] + atomicAdd(&cursor[s], 1);
-            rows[pos] = static_cast<int>(e / B);
-            vals[pos] = w[e];
-            keys[pos] = static_cast<int>(e);
+// one warp per chunk walks its entries in order; equal columns inside a
+// 32-entry group are ranked with a match mask so writes stay in (m, b) order
+__global__ void csc_place_kernel(const int64_t* __restrict__ idx, const double* __restrict__ w,
+                                 const int64_t* __restrict__ sizes, int64_t M, int64_t B, int64_t S, CscMode mode,
+                                 int* __restrict__ off, int* __restrict__ rows, double* __restrict__ vals) {
+    const int64_t c = blockIdx.x;
+    const int lane = threadIdx.x;
+    const int64_t e0 = c * CSC_CHUNK, e1 = min(M * B, e0 + CSC_CHUNK);
+    int* cur = off + c * S;
+    for (int64_t g = e0; g < e1; g += 32) {
+        const int64_t e = g + lane;
+        int64_t s = -1;
+        const bool ok = e < e1 && csc_entry(idx, sizes, e / B, e % B, B, S, mode, s, nullptr);
+        const int key = ok ? (int)s : -1 - lane;  // unique negative keys for skipped lanes
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        const int leader = __ffs(peers) - 1;
+        int basepos = 0;
+        if (ok && lane == leader) basepos = cur[s];
+        basepos = __shfl_sync(0xffffffffu, basepos, leader);
+        if (ok) {
+            rows[basepos + rank] = static_cast<int>(e / B);
+            vals[basepos + rank] = w[e];
         }
-    }
-}
-
-// sort each column's entries by (m, b): the reference's loop order
-__global__ void csc_sort_kernel(const int* __restrict__ colptr, int64_t S, int* __restrict__ rows,
-                                double* __restrict__ vals, int* __restrict__ keys) {
-    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < S; s += (int64_t)gridDim.x * blockDim.x) {
-        const int b = colptr[s], e = colptr[s + 1];
-        for (int i = b + 1; i < e; ++i) {
-            const int k = keys[i], r = rows[i];
-            const double v = vals[i];
-            int j = i - 1;
-            while (j >= b && keys[j] > k) {
-                keys[j + 1] = keys[j];
-                rows[j + 1] = rows[j];
-                vals[j + 1] = vals[j];
-                --j;
-            }
-            keys[j + 1] = k;
-            rows[j + 1] = r;
-            vals[j + 1] = v;
-        }
+        __syncwarp();
+        if (ok && lane == leader) cur[s] = basepos + __popc(peers);
+        __syncwarp();
     }
 }
 
@@ -228,6 +242,60 @@ __global__ void __launch_bounds__(256)
         acc.w = fmaf(a, x.w, acc.w);
     }
     *reinterpret_cast<float4*>(out + s * ld_out + c0) = acc;
+}
+
+// double-float version: 4 consecutive columns per thread (scalar loads; the
+// float4 path below is used when rows are 16-byte aligned)
+template <bool VEC>
+__global__ void __launch_bounds__(256)
+    csc_spmm_t_df_kernel(const int* __restrict__ colptr, const int* __restrict__ rows, const double* __restrict__ vals,
+                         const float* __restrict__ Xh, const float* __restrict__ Xl, int64_t ld_x, int64_t cols,
+                         float* __restrict__ Oh, float* __restrict__ Ol, int64_t ld_out) {
+    const int64_t s = blockIdx.x;
+    const int64_t c0 = (blockIdx.y * (int64_t)blockDim.x + threadIdx.x) * 4;
+    if (c0 >= cols) return;
+    const int b = colptr[s], e = colptr[s + 1];
+    df acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    int q = b;
+    if (VEC) {
+        // four entries' rows in flight at once
+        for (; q + 4 <= e; q += 4) {
+            float4 h[4], l[4];
+            df a[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int64_t off = (int64_t)rows[q + u] * ld_x + c0;
+                h[u] = __ldg(reinterpret_cast<const float4*>(Xh + off));
+                l[u] = __ldg(reinterpret_cast<const float4*>(Xl + off));
+                a[u] = df_from(vals[q + u]);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                df_fma_acc(acc[0], a[u], {h[u].x, l[u].x});
+                df_fma_acc(acc[1], a[u], {h[u].y, l[u].y});
+                df_fma_acc(acc[2], a[u], {h[u].z, l[u].z});
+                df_fma_acc(acc[3], a[u], {h[u].w, l[u].w});
+            }
+        }
+    }
+    for (; q < e; ++q) {
+        const df a = df_from(vals[q]);
+        const int64_t off = (int64_t)rows[q] * ld_x + c0;
+        if (VEC) {
+            const float4 h = __ldg(reinterpret_cast<const float4*>(Xh + off));
+            const float4 l = __ldg(reinterpret_cast<const float4*>(Xl + off));
+            df_fma_acc(acc[0], a, {h.x, l.x});
+            df_fma_acc(acc[1], a, {h.y, l.y});
+            df_fma_acc(acc[2], a, {h.z, l.z});
+            df_fma_acc(acc[3], a, {h.w, l.w});
+        } else {
+            for (int v = 0; v < 4 && c0 + v < cols; ++v) df_fma_acc(acc[v], a, {__ldg(Xh + off + v), __ldg(Xl + off + v)});
+        }
+    }
+    for (int v = 0; v < 4 && c0 + v < cols; ++v) {
+        Oh[s * ld_out + c0 + v] = acc[v].hi;
+        Ol[s * ld_out + c0 + v] = acc[v].lo;
+    }
 }
 
 __global__ void csc_spmv_t_kernel(const int* __restrict__ colptr, const int* __restrict__ rows,
@@ -349,35 +417,40 @@ int regularization(double coefficient, const double* coefficient_dev, const int6
     return check_launch();
 }
 
+inline int64_t csc_chunks(int64_t M, int64_t B) { return (M * B + CSC_CHUNK - 1) / CSC_CHUNK; }
+
 size_t csc_bytes(int64_t M, int64_t B, int64_t S) {
+    const int64_t nch = csc_chunks(M, B) > 0 ? csc_chunks(M, B) : 1;
     Sizer s;
     s.take<int>(S + 1);
     s.take<int>(M * B);
     s.take<double>(M * B);
-    s.take<int>(M * B);
-    s.take<int>(S);
+    s.take<int>(nch * S);  // hist
+    s.take<int>(nch * S);  // offsets / cursors
     return s.total();
 }
 
 void csc_take(Carver& cv, int64_t M, int64_t B, int64_t S, Csc& c) {
+    const int64_t nch = csc_chunks(M, B) > 0 ? csc_chunks(M, B) : 1;
     c.colptr = cv.take<int>(S + 1);
     c.rows = cv.take<int>(M * B);
     c.vals = cv.take<double>(M * B);
-    c.keys = cv.take<int>(M * B);
-    c.cursor = cv.take<int>(S);
+    c.keys = cv.take<int>(nch * S);
+    c.cursor = cv.take<int>(nch * S);
 }
 
 int csc_build(const int64_t* idx, const double* w, const int64_t* sizes, int64_t M, int64_t B, int64_t S, CscMode mode,
               Csc& c, int* info, cudaStream_t st) {
-    if (cudaMemsetAsync(c.cursor, 0, sizeof(int) * S, st) != cudaSuccess) return AJ_ERR_CUDA;
-    const unsigned g = blocks_for(M * B, 256, 16 * num_sms());
-    csc_count_kernel<<<g, 256, 0, st>>>(idx, sizes, M, B, S, mode, c.cursor, info);
+    const int64_t nch = csc_chunks(M, B);
+    if (nch == 0) return cudaMemsetAsync(c.colptr, 0, sizeof(int) * (S + 1), st) == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+    int* hist = c.keys;
+    int* off = c.cursor;
+    if (cudaMemsetAsync(hist, 0, sizeof(int) * nch * S, st) != cudaSuccess) return AJ_ERR_CUDA;
+    csc_hist_kernel<<<(unsigned)nch, 256, 0, st>>>(idx, sizes, M, B, S, mode, hist, info);
     AJ_LAUNCHED();
-    csc_scan_kernel<<<1, 1024, 0, st>>>(c.cursor, S, c.colptr);
+    csc_offsets_kernel<<<1, 1024, 0, st>>>(hist, nch, S, c.colptr, off);
     AJ_LAUNCHED();
-    csc_fill_kernel<<<g, 256, 0, st>>>(idx, w, sizes, M, B, S, mode, c.colptr, c.cursor, c.rows, c.vals, c.keys, info);
-    AJ_LAUNCHED();
-    csc_sort_kernel<<<blocks_for(S, 128, 8 * num_sms()), 128, 0, st>>>(c.colptr, S, c.rows, c.vals, c.keys);
+    csc_place_kernel<<<(unsigned)nch, 32, 0, st>>>(idx, w, sizes, M, B, S, mode, off, c.rows, c.vals);
     return check_launch();
 }
 
@@ -406,6 +479,19 @@ template int csc_spmm_t<float, float>(const Csc&, int64_t, const float*, int64_t
                                       cudaStream_t);
 template int csc_spmm_t<float, double>(const Csc&, int64_t, const float*, int64_t, int64_t, double*, int64_t,
                                        cudaStream_t);
+
+int csc_spmm_t_df(const Csc& c, int64_t S, const float* Xh, const float* Xl, int64_t ld_x, int64_t cols, float* Oh,
+                  float* Ol, int64_t ld_out, cudaStream_t st) {
+    if (S == 0 || cols == 0) return AJ_OK;
+    dim3 grid((unsigned)S, (unsigned)((cols / 4 + 1 + 255) / 256));
+    const bool vec = (cols % 4 == 0) && (ld_x % 4 == 0) && (reinterpret_cast<uintptr_t>(Xh) % 16 == 0) &&
+                     (reinterpret_cast<uintptr_t>(Xl) % 16 == 0);
+    if (vec)
+        csc_spmm_t_df_kernel<true><<<grid, 256, 0, st>>>(c.colptr, c.rows, c.vals, Xh, Xl, ld_x, cols, Oh, Ol, ld_out);
+    else
+        csc_spmm_t_df_kernel<false><<<grid, 256, 0, st>>>(c.colptr, c.rows, c.vals, Xh, Xl, ld_x, cols, Oh, Ol, ld_out);
+    return check_launch();
+}
 
 int csc_spmv_t(const Csc& c, int64_t S, const double* x, double* out, cudaStream_t st) {
     csc_spmv_t_kernel<<<blocks_for(S, 256, 4 * num_sms()), 256, 0, st>>>(c.colptr, c.rows, c.vals, S, x, out);

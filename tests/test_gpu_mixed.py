@@ -1,0 +1,89 @@
+"""The mixed-precision path (double-float on the float32 pipe) against the float64 oracle.
+
+Tolerances (stated per result, as the mixed path promises): logE rel 1e-8;
+dlogE/dlambda within 1e-6 of the scale of its two cancelling traces
+(tr(H^-1 L) ~ S / lambda) plus 1e-5 relative; weight gradient 1e-5 of its
+largest entry.  Double-float keeps ~2^-47 per operation; the fixtures reach
+condition numbers near 1e12, which is where these bounds come from.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import golden_util as gu
+from oracle import adjoint
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def aj():
+    import autojax_gb300
+
+    return autojax_gb300
+
+
+def _args(d):
+    return (d["dirty_image"], d["data"], d["noise_map"], d["w_tilde"], d["pix_indexes_for_sub_slim_index"],
+            d["pix_weights_for_sub_slim_index"], d["neighbors"], d["neighbors_sizes"])
+
+
+@pytest.mark.parametrize("case", gu.CASES)
+@pytest.mark.parametrize("coef", [0.05, 1.0, 20.0])
+def test_mixed_matches_oracle(aj, case, coef):
+    d = gu.full_inputs(case)
+    logE, dlam, gw = aj.log_evidence_and_grad(*_args(d), coefficient=coef, precision="mixed")
+    r_logE, r_dlam, r_gw = adjoint.log_evidence_and_grad(*_args(d), coefficient=coef)
+    assert abs(logE - r_logE) <= 1e-8 * abs(r_logE), (logE, r_logE)
+    trace_scale = d["pixels"] / coef**2
+    assert abs(dlam - r_dlam) <= 1e-6 * trace_scale + 1e-5 * abs(r_dlam), (dlam, r_dlam)
+    np.testing.assert_allclose(gw, r_gw, rtol=0, atol=1e-5 * np.abs(r_gw).max())
+
+
+@pytest.mark.parametrize("case", ["cfg1", "edge"])
+def test_mixed_compact_matches_oracle(aj, case):
+    d = gu.full_inputs(case)
+    a = _args(d)
+    got = aj.log_likelihood_function_via_w_compact_from(a[0], a[1], a[2], d["w_compact"],
+                                                        d["native_index_for_slim_index"], *a[4:], precision="mixed")
+    exp = float(gu.expected(case, "numba__log_likelihood_function_via_w_compact_from"))
+    assert abs(got - exp) <= 1e-8 * abs(exp)
+
+
+def test_evaluator_graph_replay_matches_direct(aj):
+    import torch
+
+    from autojax_gb300.inversion import LogEvidence
+
+    d = gu.full_inputs("cfg1")
+    a = _args(d)
+    ev = LogEvidence(a[0], a[1], a[2], a[3], S=d["pixels"], B=a[4].shape[1], P=a[6].shape[1], precision="mixed")
+    ev.set_model(a[4], a[5], a[6], a[7], coefficient=0.7)
+    ev.capture()
+    for coef in (0.7, 0.2, 3.0):
+        logE, dlam, gw = ev.evaluate_host(a[4], a[5], a[6], a[7], coef)
+        r = adjoint.log_evidence_and_grad(*a, coefficient=coef)
+        assert abs(logE - r[0]) <= 1e-8 * abs(r[0])
+        assert abs(dlam - r[1]) <= 1e-7 * d["pixels"] / coef**2 + 1e-6 * abs(r[1])
+    assert ev.launches_per_eval and ev.launches_per_eval > 10
+
+
+def test_autograd_function(aj):
+    import torch
+
+    from autojax_gb300.inversion import LogEvidence, log_evidence
+
+    d = gu.full_inputs("edge")
+    a = _args(d)
+    ev = LogEvidence(a[0], a[1], a[2], a[3], S=d["pixels"], B=a[4].shape[1], P=a[6].shape[1], precision="fp64")
+    ev.set_model(a[4], a[5], a[6], a[7], coefficient=1.0)
+    w = torch.tensor(a[5], device="cuda", requires_grad=True)
+    c = torch.tensor(1.3, dtype=torch.float64, device="cuda", requires_grad=True)
+    out = log_evidence(w, c, ev)
+    out.backward()
+    r = adjoint.log_evidence_and_grad(*a, coefficient=1.3)
+    assert abs(float(out) - r[0]) <= 1e-10 * abs(r[0])
+    np.testing.assert_allclose(w.grad.cpu().numpy(), r[2], rtol=1e-8, atol=1e-9 * np.abs(r[2]).max())
+    assert abs(float(c.grad) - 2 * 1.3 * r[1]) <= 1e-7 * max(1.0, abs(2 * 1.3 * r[1]))
