@@ -54,6 +54,10 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
             bool lower_only, bool tri_k, cudaStream_t st);
 int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* logdet, int* info, cudaStream_t st);
 int dfspd_invert_factor(int64_t S, DfSpd& w, cudaStream_t st);
+// the same for count = 1 or 2 independent matrices sharing every launch
+int dfspd_factor_n(const float* const* Ah, const float* const* Al, int count, int64_t S, DfSpd* const* w,
+                   double* const* logdet, int* info, cudaStream_t st);
+int dfspd_invert_factor_n(int64_t S, DfSpd* const* w, int count, cudaStream_t st);
 int dfspd_inverse_from_factor(int64_t S, DfSpd& w, float* Ah, float* Al, cudaStream_t st);
 int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st);
 int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x, double* r,

@@ -441,9 +441,13 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         AJ_LAUNCHED();
         split_shifted_kernel<<<blocks_for(S * S, 256, 8 * num_sms()), 256, 0, st>>>(b.H, S, b.logdets + 4, b.Hh, b.Hl);
         AJ_LAUNCHED();
-        AJ_TRY(dfspd_factor(b.Ah, b.Al, S, b.da, b.logdets + 0, info, st));
-        AJ_TRY(dfspd_factor(b.Hh, b.Hl, S, b.dh, b.logdets + 1, info, st));
-        AJ_TRY(dfspd_invert_factor(S, b.da, st));
+        // A and H share every factorisation launch (and, with the gradient, every inversion launch)
+        const float* fh[2] = {b.Ah, b.Hh};
+        const float* fl[2] = {b.Al, b.Hl};
+        DfSpd* fw[2] = {&b.da, &b.dh};
+        double* ld[2] = {b.logdets + 0, b.logdets + 1};
+        AJ_TRY(dfspd_factor_n(fh, fl, 2, S, fw, ld, info, st));
+        AJ_TRY(dfspd_invert_factor_n(S, fw, with_grad ? 2 : 1, st));
         AJ_TRY(dfspd_solve_refined(S, b.da, b.Ah, b.Al, b.D, b.s, b.res, st));
     }
 
@@ -473,7 +477,6 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         AJ_TRY(dfspd_inverse_from_factor(S, b.da, b.AIh, b.AIl, st));
         AJ_TRY(df_join(b.AIh, b.AIl, S * S, b.Ainv, st));
         AJ_TRY(df_join(b.Omh, b.Oml, M * S, b.Om, st));
-        AJ_TRY(dfspd_invert_factor(S, b.dh, st));
         AJ_TRY(df_frob_lower(b.dh.Ih, b.dh.Il, S, b.fpart, b.nfrob, st));
     }
     dlam_kernel<<<1, 1024, 0, st>>>(p->neighbors, p->neighbors_sizes, S, p->P, b.s, b.Ainv, b.fpart, b.nfrob,

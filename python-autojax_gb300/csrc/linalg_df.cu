@@ -21,6 +21,19 @@ namespace aj {
 
 constexpr int DNB = 32;
 
+// Up to two independent matrices factored or inverted by the same launches
+// (blockIdx.y picks one): the evaluation's A and H share every step, which
+// halves the serial chain of small launches and doubles their parallelism.
+struct DfMats {
+    float* Lh[2];
+    float* Ll[2];
+    float* Ih[2];
+    float* Il[2];
+    float* dh[2];
+    float* dl[2];
+    double* piv[2];
+};
+
 __device__ __forceinline__ df dfmul(df a, df b) {
     const float p = a.hi * b.hi;
     float e = fmaf(a.hi, b.hi, -p);
@@ -268,8 +281,14 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 // update (two barriers a column), and the inverse spreads each column's
 // substitution over 8 threads whose partial dot products meet in shuffles.
 __global__ void __launch_bounds__(256)
-    dfchol_panel_kernel(float* __restrict__ Lh, float* __restrict__ Ll, int64_t S, int64_t k0,
-                        float* __restrict__ dh, float* __restrict__ dl, double* __restrict__ piv, int* info) {
+    dfchol_panel_kernel(DfMats mats, int64_t S, int64_t k0, int* info) {
+    const int z = blockIdx.y;
+    float* __restrict__ Lh = mats.Lh[z];
+    float* __restrict__ Ll = mats.Ll[z];
+    const int64_t kb = k0 / DNB;
+    float* __restrict__ dh = mats.dh[z] + kb * DNB * DNB;
+    float* __restrict__ dl = mats.dl[z] + kb * DNB * DNB;
+    double* __restrict__ piv = mats.piv[z];
     __shared__ float ah[DNB][DNB + 1], al[DNB][DNB + 1];
     __shared__ float ih[DNB][DNB + 1], il[DNB][DNB + 1];
     __shared__ float lh[DNB][DNB + 1], ll[DNB][DNB + 1];
@@ -416,7 +435,9 @@ __global__ void __launch_bounds__(256)
 // outputs each; small register and shared footprint so several blocks share
 // an SM and the late, small steps still fill the GPU.
 __global__ void __launch_bounds__(128)
-    dfsyrk_update_kernel(float* __restrict__ Lh, float* __restrict__ Ll, int64_t S, int64_t k0) {
+    dfsyrk_update_kernel(DfMats mats, int64_t S, int64_t k0) {
+    float* __restrict__ Lh = mats.Lh[blockIdx.y];
+    float* __restrict__ Ll = mats.Ll[blockIdx.y];
     __shared__ float pih[32][33], pil[32][33], pjh[32][33], pjl[32][33];
     const int64_t r0 = k0 + DNB;
     int64_t ti, tj;
@@ -488,8 +509,11 @@ __global__ void df_logdet_kernel(const double* __restrict__ piv, int64_t S, doub
 
 // ---------------------------------------------------- triangular inverse
 
-__global__ void df_linv_init_kernel(float* __restrict__ Ih, float* __restrict__ Il, int64_t S,
-                                    const float* __restrict__ dh, const float* __restrict__ dl) {
+__global__ void df_linv_init_kernel(DfMats mats, int64_t S) {
+    float* __restrict__ Ih = mats.Ih[blockIdx.y];
+    float* __restrict__ Il = mats.Il[blockIdx.y];
+    const float* __restrict__ dh = mats.dh[blockIdx.y];
+    const float* __restrict__ dl = mats.dl[blockIdx.y];
     const int64_t kb = blockIdx.x, k0 = kb * DNB;
     for (int e = threadIdx.x; e < DNB * DNB; e += blockDim.x) {
         const int i = e / DNB, j = e % DNB;
@@ -502,9 +526,13 @@ __global__ void df_linv_init_kernel(float* __restrict__ Ih, float* __restrict__ 
 
 // see trtri_step_kernel (linalg.cu): accumulate L[ti][kb] X[kb][tj]; block row kb + 1 applies -dinv
 __global__ void __launch_bounds__(256)
-    df_trtri_step_kernel(const float* __restrict__ Lh, const float* __restrict__ Ll, float* __restrict__ Ih,
-                         float* __restrict__ Il, int64_t S, int64_t kb, const float* __restrict__ dh,
-                         const float* __restrict__ dl) {
+    df_trtri_step_kernel(DfMats mats, int64_t S, int64_t kb) {
+    const float* __restrict__ Lh = mats.Lh[blockIdx.y];
+    const float* __restrict__ Ll = mats.Ll[blockIdx.y];
+    float* __restrict__ Ih = mats.Ih[blockIdx.y];
+    float* __restrict__ Il = mats.Il[blockIdx.y];
+    const float* __restrict__ dh = mats.dh[blockIdx.y];
+    const float* __restrict__ dl = mats.dl[blockIdx.y];
     __shared__ float ah[32][33], al[32][33], bh[32][33], bl[32][33];
     const int64_t nbt = (S + DNB - 1) / DNB;
     const int64_t ncol = kb + 1;
@@ -674,51 +702,87 @@ int df_add_f64(const float* ah, const float* al, const double* b, int64_t n, flo
     return check_launch();
 }
 
-// L (in w) = chol(A); A given as planes (copied unless it is w's own L)
-int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* logdet, int* info, cudaStream_t st) {
-    if (S <= 0) return AJ_OK;
-    if (Ah != w.Lh) {
-        if (cudaMemcpyAsync(w.Lh, Ah, sizeof(float) * S * S, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
-            cudaMemcpyAsync(w.Ll, Al, sizeof(float) * S * S, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
-            return AJ_ERR_CUDA;
+static DfMats mats_of(DfSpd* const* w, int count) {
+    DfMats m{};
+    for (int z = 0; z < 2; ++z) {
+        DfSpd* x = w[z < count ? z : 0];
+        m.Lh[z] = x->Lh;
+        m.Ll[z] = x->Ll;
+        m.Ih[z] = x->Ih;
+        m.Il[z] = x->Il;
+        m.dh[z] = x->dh;
+        m.dl[z] = x->dl;
+        m.piv[z] = x->piv;
     }
+    return m;
+}
+
+// L (in w[z]) = chol(A[z]) for z < count (1 or 2); A given as planes (copied unless it is w's own L)
+int dfspd_factor_n(const float* const* Ah, const float* const* Al, int count, int64_t S, DfSpd* const* w,
+                   double* const* logdet, int* info, cudaStream_t st) {
+    if (S <= 0) return AJ_OK;
+    if (count < 1 || count > 2) return AJ_ERR_ARG;
+    for (int z = 0; z < count; ++z) {
+        if (Ah[z] != w[z]->Lh) {
+            if (cudaMemcpyAsync(w[z]->Lh, Ah[z], sizeof(float) * S * S, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+                cudaMemcpyAsync(w[z]->Ll, Al[z], sizeof(float) * S * S, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+                return AJ_ERR_CUDA;
+        }
+    }
+    const DfMats m = mats_of(w, count);
     const int64_t nbt = (S + DNB - 1) / DNB;
     for (int64_t kb = 0; kb < nbt; ++kb) {
         const int64_t k0 = kb * DNB;
         const int64_t below = S - k0 - DNB;
         const unsigned g = 1 + (unsigned)(below > 0 ? (below + 63) / 64 : 0);
-        dfchol_panel_kernel<<<g, 256, 0, st>>>(w.Lh, w.Ll, S, k0, w.dh + kb * DNB * DNB, w.dl + kb * DNB * DNB, w.piv,
-                                               info);
+        dfchol_panel_kernel<<<dim3(g, count), 256, 0, st>>>(m, S, k0, info);
         AJ_LAUNCHED();
         if (below > 0) {
             const int64_t tb = (below + 31) / 32;
-            dfsyrk_update_kernel<<<(unsigned)(tb * (tb + 1) / 2), 128, 0, st>>>(w.Lh, w.Ll, S, k0);
+            dfsyrk_update_kernel<<<dim3((unsigned)(tb * (tb + 1) / 2), count), 128, 0, st>>>(m, S, k0);
             AJ_LAUNCHED();
         }
     }
     dim3 zg(blocks_for(S, 256, 8), (unsigned)(S < 65535 ? S : 65535));
-    df_zero_upper_kernel<<<zg, 256, 0, st>>>(w.Lh, w.Ll, S);
+    for (int z = 0; z < count; ++z) {
+        df_zero_upper_kernel<<<zg, 256, 0, st>>>(w[z]->Lh, w[z]->Ll, S);
+        AJ_LAUNCHED();
+        if (logdet && logdet[z]) {
+            df_logdet_kernel<<<1, 1024, 0, st>>>(w[z]->piv, S, logdet[z], info);
+            AJ_LAUNCHED();
+        }
+    }
+    return AJ_OK;
+}
+
+int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* logdet, int* info, cudaStream_t st) {
+    DfSpd* ws[1] = {&w};
+    double* ld[1] = {logdet};
+    return dfspd_factor_n(&Ah, &Al, 1, S, ws, ld, info, st);
+}
+
+int dfspd_invert_factor_n(int64_t S, DfSpd* const* w, int count, cudaStream_t st) {
+    if (S <= 0) return AJ_OK;
+    if (count < 1 || count > 2) return AJ_ERR_ARG;
+    for (int z = 0; z < count; ++z) {
+        if (!w[z]->Ih) return AJ_ERR_ARG;
+        if (cudaMemsetAsync(w[z]->Ih, 0, sizeof(float) * 2 * S * S, st) != cudaSuccess) return AJ_ERR_CUDA;
+    }
+    const DfMats m = mats_of(w, count);
+    const int64_t nbt = (S + DNB - 1) / DNB;
+    df_linv_init_kernel<<<dim3((unsigned)nbt, count), 256, 0, st>>>(m, S);
     AJ_LAUNCHED();
-    if (logdet) {
-        df_logdet_kernel<<<1, 1024, 0, st>>>(w.piv, S, logdet, info);
+    for (int64_t kb = 0; kb + 1 < nbt; ++kb) {
+        const int64_t tiles = (nbt - kb - 1) * (kb + 1);
+        df_trtri_step_kernel<<<dim3((unsigned)tiles, count), 256, 0, st>>>(m, S, kb);
         AJ_LAUNCHED();
     }
     return AJ_OK;
 }
 
 int dfspd_invert_factor(int64_t S, DfSpd& w, cudaStream_t st) {
-    if (S <= 0) return AJ_OK;
-    if (!w.Ih) return AJ_ERR_ARG;
-    const int64_t nbt = (S + DNB - 1) / DNB;
-    if (cudaMemsetAsync(w.Ih, 0, sizeof(float) * 2 * S * S, st) != cudaSuccess) return AJ_ERR_CUDA;
-    df_linv_init_kernel<<<(unsigned)nbt, 256, 0, st>>>(w.Ih, w.Il, S, w.dh, w.dl);
-    AJ_LAUNCHED();
-    for (int64_t kb = 0; kb + 1 < nbt; ++kb) {
-        const int64_t tiles = (nbt - kb - 1) * (kb + 1);
-        df_trtri_step_kernel<<<(unsigned)tiles, 256, 0, st>>>(w.Lh, w.Ll, w.Ih, w.Il, S, kb, w.dh, w.dl);
-        AJ_LAUNCHED();
-    }
-    return AJ_OK;
+    DfSpd* ws[1] = {&w};
+    return dfspd_invert_factor_n(S, ws, 1, st);
 }
 
 int dfspd_inverse_from_factor(int64_t S, DfSpd& w, float* Ah, float* Al, cudaStream_t st) {

@@ -3,8 +3,9 @@
 Tolerances (stated per result, as the mixed path promises): logE rel 1e-8;
 dlogE/dlambda within 1e-6 of the scale of its two cancelling traces
 (tr(H^-1 L) ~ S / lambda) plus 1e-5 relative; weight gradient 1e-5 of its
-largest entry.  Double-float keeps ~2^-47 per operation; the fixtures reach
-condition numbers near 1e12, which is where these bounds come from.
+largest entry, or 2e-15 cond(A) of it when larger (the gradient goes through
+A^-1).  Double-float keeps ~2^-47 per operation; the fixtures reach condition
+numbers near 1e11, which is where these bounds come from.
 """
 
 from __future__ import annotations
@@ -39,7 +40,14 @@ def test_mixed_matches_oracle(aj, case, coef):
     assert abs(logE - r_logE) <= 1e-8 * abs(r_logE), (logE, r_logE)
     trace_scale = d["pixels"] / coef**2
     assert abs(dlam - r_dlam) <= 1e-6 * trace_scale + 1e-5 * abs(r_dlam), (dlam, r_dlam)
-    np.testing.assert_allclose(gw, r_gw, rtol=0, atol=1e-5 * np.abs(r_gw).max())
+    # the weight gradient goes through A^-1: its error scales with cond(A) (refgen reaches ~1e11)
+    from oracle import numpy_port as ref
+
+    T = ref.mapping_matrix_from(d["pix_indexes_for_sub_slim_index"], d["pix_weights_for_sub_slim_index"], d["pixels"])
+    ev = np.linalg.eigvalsh(T.T @ d["w_tilde"] @ T + ref.constant_regularization_matrix_from(coef, d["neighbors"],
+                                                                                              d["neighbors_sizes"]))
+    cond = ev[-1] / ev[0]
+    np.testing.assert_allclose(gw, r_gw, rtol=0, atol=max(1e-5, 2e-15 * cond) * np.abs(r_gw).max())
 
 
 @pytest.mark.parametrize("case", ["cfg1", "edge"])
