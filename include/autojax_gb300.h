@@ -36,6 +36,7 @@ extern "C" {
 #define AJ_ERR_ARG (-1)       /* bad size, null pointer, unknown precision */
 #define AJ_ERR_CUDA (-2)      /* a launch failed; see aj_last_cuda_error() */
 #define AJ_ERR_WORKSPACE (-3) /* workspace smaller than *_workspace_size() */
+#define AJ_ERR_TOO_LARGE (-4) /* size above the fixed capacity of a no-allocation entry point */
 
 #define AJ_INFO_OK 0
 #define AJ_INFO_INDEX_RANGE 1       /* an index was outside [0, n) and not -1 */
@@ -189,6 +190,19 @@ int aj_constant_regularization(double coefficient, const int64_t* neighbors, con
 size_t aj_spd_solve_workspace_size(int64_t S);
 int aj_spd_solve(const double* data_vector, const double* A, int64_t S, double* out, void* workspace,
                  size_t workspace_bytes, int* info, void* stream);
+
+/* The solve of aj_spd_solve for callers that cannot allocate device memory
+ * (a plugin or foreign-function host that only receives device pointers, or
+ * code whose allocator belongs to someone else): no workspace argument, and no
+ * cudaMalloc, cudaFree or allocating library call. No counterpart in the
+ * reference. Scratch is one file-scope __device__ array sized for
+ * S <= AJ_NOALLOC_SOLVE_MAX_S (about 8.3 MB, held by every GPU that loads the
+ * library until the process exits); larger S returns AJ_ERR_TOO_LARGE. The
+ * first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * All calls on a device share the array: calls whose GPU work overlaps race. */
+#define AJ_NOALLOC_SOLVE_MAX_S 1024
+int aj_spd_solve_noalloc(const double* data_vector, const double* A, int64_t S, double* out, int* info, void* stream);
 
 /* log|det A| of a symmetric positive definite A (the slogdet of numba.py:849-850). */
 int aj_spd_logdet(const double* A, int64_t S, double* out, void* workspace, size_t workspace_bytes, int* info,

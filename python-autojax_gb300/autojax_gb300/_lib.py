@@ -16,6 +16,8 @@ AJ_OK = 0
 AJ_ERR_ARG = -1
 AJ_ERR_CUDA = -2
 AJ_ERR_WORKSPACE = -3
+AJ_ERR_TOO_LARGE = -4
+AJ_NOALLOC_SOLVE_MAX_S = 1024
 AJ_INFO_INDEX_RANGE = 1
 AJ_INFO_NOT_POSITIVE_DEFINITE = 2
 AJ_FP64 = 0
@@ -88,6 +90,7 @@ SIGNATURES = {
     "aj_constant_regularization": (INT, [D, P, P, I64, I64, P, P, P]),
     "aj_spd_solve_workspace_size": (SZ, [I64]),
     "aj_spd_solve": (INT, [P, P, I64, P, P, SZ, P, P]),
+    "aj_spd_solve_noalloc": (INT, [P, P, I64, P, P, P]),
     "aj_spd_logdet": (INT, [P, I64, P, P, SZ, P, P]),
     "aj_spd_inverse_workspace_size": (SZ, [I64]),
     "aj_spd_inverse": (INT, [P, I64, P, P, P, SZ, P, P]),
@@ -142,6 +145,8 @@ def check(rc: int, what: str) -> None:
         raise ValueError(f"{what}: invalid argument")
     if rc == AJ_ERR_WORKSPACE:
         raise RuntimeError(f"{what}: workspace too small")
+    if rc == AJ_ERR_TOO_LARGE:
+        raise ValueError(f"{what}: size above the entry point's fixed capacity")
     if rc == AJ_ERR_CUDA:
         raise RuntimeError(f"{what}: CUDA launch failed (cudaError {lib.aj_last_cuda_error()})")
     raise RuntimeError(f"{what}: status {rc}")

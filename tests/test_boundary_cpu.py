@@ -47,7 +47,7 @@ def test_status_codes_match_header():
     from autojax_gb300 import _lib
 
     text = HEADER.read_text()
-    for name in ("AJ_OK", "AJ_ERR_ARG", "AJ_ERR_CUDA", "AJ_ERR_WORKSPACE", "AJ_INFO_INDEX_RANGE",
+    for name in ("AJ_OK", "AJ_ERR_ARG", "AJ_ERR_CUDA", "AJ_ERR_WORKSPACE", "AJ_ERR_TOO_LARGE", "AJ_INFO_INDEX_RANGE",
                  "AJ_INFO_NOT_POSITIVE_DEFINITE", "AJ_FP64", "AJ_MIXED"):
         m = re.search(rf"#define {name} \(?(-?\d+)\)?", text)
         assert m, name
