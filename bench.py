@@ -298,37 +298,43 @@ def gpu_arm(args, dist: Dist) -> dict:
         e.evaluate_host(*mods[i % len(mods)])
     t_e2e = dist.max(time.perf_counter() - t0)
 
-    # roofline of the dominant kernel group: the float64 blocked Cholesky / inverse (measured standalone)
+    # Roofline of the dominant kernel group of the headline (mixed) path: the double-float
+    # factorisation kernels (Cholesky panel + trailing update + triangular inverse, plus
+    # L^-T L^-1), timed standalone on this workload's A with CUDA events.  Algorithmic work
+    # S^3 (S^3/3 each for the factor, the inverse factor and L^-T L^-1) in float64-class
+    # flops; the double-float peak is the measured float32 FMA rate over the 11.4 float32
+    # instructions one double-float multiply-add takes (2 flops).
     A = torch.from_numpy(aj.constant_regularization_matrix_from(1.0, d["neighbors"], d["neighbors_sizes"])).to(dev)
     F = aj.curvature_matrix_via_w_wilde_sparse_mapping_matrix_from(
         w_tilde, torch.from_numpy(d["pix_indexes_for_sub_slim_index"]).to(dev),
         torch.from_numpy(d["pix_weights_for_sub_slim_index"]).to(dev), S)
     A = (A + F).contiguous()
-    ws = torch.empty(lib.aj_spd_inverse_workspace_size(S), dtype=torch.uint8, device=dev)
     Ainv = torch.empty((S, S), dtype=torch.float64, device=dev)
     ld = torch.empty(1, dtype=torch.float64, device=dev)
     info = torch.zeros(2, dtype=torch.int32, device=dev)
     stc = torch.cuda.current_stream().cuda_stream
+    ws_m = torch.empty(lib.aj_spd_inverse_mixed_workspace_size(S), dtype=torch.uint8, device=dev)
+    ws_f = torch.empty(lib.aj_spd_inverse_workspace_size(S), dtype=torch.uint8, device=dev)
 
-    def inv_call(i):
-        _lib.check(lib.aj_spd_inverse(A.data_ptr(), S, Ainv.data_ptr(), ld.data_ptr(), ws.data_ptr(), ws.numel(),
+    def inv_mixed(i):
+        _lib.check(lib.aj_spd_inverse_mixed(A.data_ptr(), S, Ainv.data_ptr(), ld.data_ptr(), ws_m.data_ptr(),
+                                            ws_m.numel(), info.data_ptr(), stc), "aj_spd_inverse_mixed")
+
+    def inv_fp64(i):
+        _lib.check(lib.aj_spd_inverse(A.data_ptr(), S, Ainv.data_ptr(), ld.data_ptr(), ws_f.data_ptr(), ws_f.numel(),
                                       info.data_ptr(), stc), "aj_spd_inverse")
 
-    def chol_call(i):
-        _lib.check(lib.aj_spd_logdet(A.data_ptr(), S, ld.data_ptr(), ws.data_ptr(), ws.numel(), info.data_ptr(), stc),
-                   "aj_spd_logdet")
-
     for i in range(2):
-        inv_call(i)
+        inv_mixed(i)
+        inv_fp64(i)
     reps = 5
-    t_chol = time_region(chol_call, reps, dist) / reps
-    t_inv = time_region(inv_call, reps, dist) / reps
+    t_inv_mixed = time_region(inv_mixed, reps, dist, "roofline_mixed") / reps
+    t_inv_fp64 = time_region(inv_fp64, reps, dist, "roofline_fp64") / reps
     fp64_peak = fma_peak_tflops(_lib.AJ_FP64)
     fp32_peak = fma_peak_tflops(_lib.AJ_MIXED)
-    # algorithmic flops: Cholesky S^3/3, triangular inverse S^3/3, L^-T L^-1 S^3/3
-    chol_flops = S**3 / 3.0
-    inv_flops = S**3
-    achieved = inv_flops / t_inv / 1e12
+    df_peak = fp32_peak / 11.4
+    inv_flops = float(S) ** 3
+    achieved = inv_flops / t_inv_mixed / 1e12
 
     result = {
         "metric": METRIC,
@@ -358,17 +364,19 @@ def gpu_arm(args, dist: Dist) -> dict:
                 "d2h_bytes_per_step": e.d2h_bytes()},
         "gpu_launches": (ev["mixed"].launches_per_eval or 0) * args.steps,
         "roofline": {
-            "kernel": "blocked float64 Cholesky + triangular inverse + L^-T L^-1 (aj_spd_inverse; gemm_f64 tiles)",
-            "bound": "fp64",
+            "kernel": "double-float Cholesky + triangular inverse + L^-T L^-1 of A (aj_spd_inverse_mixed: "
+                      "dfchol_panel, dfsyrk_update, df_trtri_step, gemm_df)",
+            "bound": "fp32 (double-float)",
             "achieved": achieved,
-            "peak": fp64_peak,
-            "unit": "TFLOP/s",
-            "frac": achieved / fp64_peak,
-            "peak_source": "measured in this run (aj_probe_fma float64 FMA loop)",
+            "peak": df_peak,
+            "unit": "TFLOP/s (float64-class)",
+            "frac": achieved / df_peak,
+            "peak_source": "measured in this run: aj_probe_fma float32 FMA rate / 11.4 float32 instructions "
+                           "per double-float multiply-add",
             "traffic": None,
-            "cholesky_ms": 1e3 * t_chol,
-            "cholesky_tflops": chol_flops / t_chol / 1e12,
-            "inverse_ms": 1e3 * t_inv,
+            "ms": 1e3 * t_inv_mixed,
+            "fp64_same_work_ms": 1e3 * t_inv_fp64,
+            "fp64_same_work_frac_of_fp64_peak": inv_flops / t_inv_fp64 / 1e12 / fp64_peak,
         },
         "peaks": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak,
                   "hbm_gbs": measured_peaks().get("hbm_gbs"), "bf16_tflops": measured_peaks().get("bf16_tflops")},
@@ -382,41 +390,46 @@ def gpu_arm(args, dist: Dist) -> dict:
 
 
 def wtilde_bench(d, dev, fp32_peak) -> dict:
-    """Direct w_tilde kernel (numba.py:156-207) on the workload's M with a visibility sample."""
+    """Direct w_tilde build (numba.py:156-207) on the workload's M with a visibility sample.
+
+    The mixed build does 2 double-float multiply-adds per unique (pixel pair,
+    visibility) term, 11.4 float32 instructions each; `fp32_pipe_frac` is the
+    float32 FMA-pipe share those instructions imply (ncu's pipe counters for
+    the same kernel are in the profiles).
+    """
     import torch
 
     from autojax_gb300 import _lib
 
     lib = _lib.load()
-    Ks = 16384
+    Ks = 8192
     g = torch.from_numpy(d["grid_radians_slim"]).to(dev)
     uv = torch.from_numpy(d["uv_wavelengths"][:Ks].copy()).to(dev)
     n = torch.from_numpy(d["noise_map_real"][:Ks].copy()).to(dev)
     M = g.shape[0]
-    out = {}
-    for name, pc in (("mixed", _lib.AJ_MIXED),):
-        W = torch.empty((M, M), dtype=torch.float64, device=dev)
-        ws = torch.empty(lib.aj_w_tilde_curvature_workspace_size(Ks, M, pc), dtype=torch.uint8, device=dev)
-        st = torch.cuda.current_stream()
+    W = torch.empty((M, M), dtype=torch.float64, device=dev)
+    planes = torch.empty((2, M, M), dtype=torch.float32, device=dev)
+    pc = _lib.AJ_MIXED
+    ws = torch.empty(lib.aj_w_tilde_curvature_workspace_size(Ks, M, pc), dtype=torch.uint8, device=dev)
+    st = torch.cuda.current_stream()
 
-        def call():
-            _lib.check(lib.aj_w_tilde_curvature(n.data_ptr(), uv.data_ptr(), g.data_ptr(), Ks, M, W.data_ptr(), None,
-                                                ws.data_ptr(), ws.numel(), pc, st.cuda_stream), "aj_w_tilde_curvature")
+    def call():
+        _lib.check(lib.aj_w_tilde_curvature(n.data_ptr(), uv.data_ptr(), g.data_ptr(), Ks, M, W.data_ptr(),
+                                            planes.data_ptr(), ws.data_ptr(), ws.numel(), pc, st.cuda_stream),
+                   "aj_w_tilde_curvature")
 
-        call()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        call()
-        e1.record(st)
-        e1.synchronize()
-        sec = e0.elapsed_time(e1) / 1e3
-        terms = M * (M + 1) / 2 * Ks
-        # the symmetric product does 2 FMA (4 flops) per unique (pair, visibility) term
-        flops = 4.0 * terms
-        out[name] = {"K_sample": Ks, "M": M, "seconds": sec, "terms_per_s": terms / sec,
-                     "fp32_tflops": flops / sec / 1e12, "fp32_frac": flops / sec / 1e12 / fp32_peak}
-    return out
+    call()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    call()
+    e1.record(st)
+    e1.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    terms = M * (M + 1) / 2 * Ks
+    fp32_flops = terms * 2 * 11.4 * 2
+    return {"precision": "mixed (float64 panel, double-float product)", "K_sample": Ks, "M": M, "seconds": sec,
+            "terms_per_s": terms / sec, "fp32_pipe_frac": fp32_flops / sec / 1e12 / fp32_peak}
 
 
 def stage_times(d, w_tilde, dev, dist) -> dict:

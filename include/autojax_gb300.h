@@ -79,11 +79,13 @@ int aj_slim_from_mask(const uint8_t* mask, int64_t ny, int64_t nx, const double*
  * x = grid[:,1] with u = uv[:,0], y = grid[:,0] with v = uv[:,1].
  * Computed as the K-deep symmetric product C C^T + S S^T of the
  * sqrt(w)-scaled cos/sin panels (exact identity cos(a-b) = cos a cos b +
- * sin a sin b). out64 (M, M) is always written; out32 (M, M, may be NULL)
- * receives a float copy for the mixed pipeline. */
+ * sin a sin b). out64 (M, M) is always written; out_planes (2, M, M), may
+ * be NULL, receives the double-float planes (hi then lo) the mixed
+ * likelihood reads. AJ_MIXED evaluates the panel in float64 and the product
+ * in double-float on the float32 pipe. */
 size_t aj_w_tilde_curvature_workspace_size(int64_t K, int64_t M, int precision);
 int aj_w_tilde_curvature(const double* noise_map_real, const double* uv, const double* grid_slim, int64_t K,
-                         int64_t M, double* out64, float* out32, void* workspace, size_t workspace_bytes,
+                         int64_t M, double* out64, float* out_planes, void* workspace, size_t workspace_bytes,
                          int precision, void* stream);
 
 /* numba.py:211-234 w_compact_curvature_interferometer_from.
@@ -214,6 +216,12 @@ int aj_spd_logdet(const double* A, int64_t S, double* out, void* workspace, size
 size_t aj_spd_inverse_workspace_size(int64_t S);
 int aj_spd_inverse(const double* A, int64_t S, double* Ainv, double* logdet, void* workspace, size_t workspace_bytes,
                    int* info, void* stream);
+
+/* The same as aj_spd_inverse in double-float arithmetic on the float32 pipe
+ * (A and A^-1 stay float64 in memory; ~2^-47 relative rounding per operation). */
+size_t aj_spd_inverse_mixed_workspace_size(int64_t S);
+int aj_spd_inverse_mixed(const double* A, int64_t S, double* Ainv, double* logdet, void* workspace,
+                         size_t workspace_bytes, int* info, void* stream);
 
 /* numba.py:735-752 noise_normalization_complex_from: *out = 2 (K log 2pi + sum log|Re| + sum log|Im|). */
 int aj_noise_normalization(const double* noise_map_c128, int64_t K, double* out, void* stream);

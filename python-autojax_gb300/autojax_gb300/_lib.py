@@ -94,6 +94,8 @@ SIGNATURES = {
     "aj_spd_logdet": (INT, [P, I64, P, P, SZ, P, P]),
     "aj_spd_inverse_workspace_size": (SZ, [I64]),
     "aj_spd_inverse": (INT, [P, I64, P, P, P, SZ, P, P]),
+    "aj_spd_inverse_mixed_workspace_size": (SZ, [I64]),
+    "aj_spd_inverse_mixed": (INT, [P, I64, P, P, P, SZ, P, P]),
     "aj_noise_normalization": (INT, [P, I64, P, P]),
     "aj_split_f64": (INT, [P, I64, P, P, P]),
     "aj_log_evidence_workspace_size": (SZ, [C.POINTER(Problem), INT, INT]),

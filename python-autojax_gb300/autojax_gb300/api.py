@@ -97,8 +97,12 @@ def w_tilde_data_interferometer_from(visibilities_real, noise_map_real, uv_wavel
 
 
 def w_tilde_curvature_interferometer_from(noise_map_real, uv_wavelengths, grid_radians_slim, *, precision="fp64",
-                                          out32=False):
-    """numba.py:156-207 — dense (M, M) w_tilde.  ``out32=True`` also returns a float32 copy."""
+                                          planes=False):
+    """numba.py:156-207 — dense (M, M) w_tilde.
+
+    ``planes=True`` also returns its (2, M, M) double-float planes (hi, lo), the
+    form the mixed-precision likelihood reads.
+    """
     c = Call("w_tilde_curvature_interferometer_from")
     n = c.arr(noise_map_real, f64, 1, "noise_map_real")
     uv = c.arr(uv_wavelengths, f64, 2, "uv_wavelengths")
@@ -106,11 +110,11 @@ def w_tilde_curvature_interferometer_from(noise_map_real, uv_wavelengths, grid_r
     K, M = uv.shape[0], g.shape[0]
     pc = precision_code(precision)
     out = c.empty((M, M))
-    o32 = c.empty((M, M), torch.float32) if out32 else None
+    pl = c.empty((2, M, M), torch.float32) if planes else None
     ws = c.workspace(_lib.load().aj_w_tilde_curvature_workspace_size(K, M, pc))
-    _lib_call("aj_w_tilde_curvature", ptr(n), ptr(uv), ptr(g), K, M, ptr(out), ptr(o32), ptr(ws), ws.numel(), pc,
+    _lib_call("aj_w_tilde_curvature", ptr(n), ptr(uv), ptr(g), K, M, ptr(out), ptr(pl), ptr(ws), ws.numel(), pc,
               c.stream())
-    return (c.out(out), c.out(o32)) if out32 else c.out(out)
+    return (c.out(out), c.out(pl)) if planes else c.out(out)
 
 
 def w_compact_curvature_interferometer_from(grid_size, noise_map_real, uv_wavelengths, pixel_scale, *,

@@ -47,6 +47,7 @@ struct DfSpd {
 size_t dfspd_bytes(int64_t S, bool with_inverse);
 DfSpd dfspd_carve(Carver& cv, int64_t S, bool with_inverse);
 int df_split(const double* x, int64_t n, float* hi, float* lo, cudaStream_t st);
+int df_mirror_lower(float* hi, float* lo, int64_t S, cudaStream_t st);
 int df_join(const float* hi, const float* lo, int64_t n, double* x, cudaStream_t st);
 int df_add_f64(const float* ah, const float* al, const double* b, int64_t n, float* oh, float* ol, cudaStream_t st);
 int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const float* Ah, const float* Al, int64_t lda,
@@ -75,6 +76,7 @@ struct Csc {
     int* colptr;   // S + 1
     int* rows;     // nnz capacity M * B
     double* vals;  // nnz capacity
+    float2* vdf;   // the same weights as double-float (hi, lo), converted once at build
     int* keys;     // scratch: per-chunk column histograms
     int* cursor;   // scratch: per-chunk column write offsets
 };

@@ -687,6 +687,12 @@ DfSpd dfspd_carve(Carver& cv, int64_t S, bool with_inverse) {
     return w;
 }
 
+int df_mirror_lower(float* hi, float* lo, int64_t S, cudaStream_t st) {
+    dim3 g(blocks_for(S, 256, 8), (unsigned)(S < 65535 ? S : 65535));
+    df_mirror_lower_kernel<<<g, 256, 0, st>>>(hi, lo, S);
+    return check_launch();
+}
+
 int df_split(const double* x, int64_t n, float* hi, float* lo, cudaStream_t st) {
     split_kernel<<<blocks_for(n, 256, 8 * num_sms()), 256, 0, st>>>(x, n, hi, lo);
     return check_launch();
@@ -820,3 +826,37 @@ int df_frob_lower(const float* h, const float* l, int64_t S, double* partial, in
 }
 
 }  // namespace aj
+
+using namespace aj;
+
+extern "C" {
+
+size_t aj_spd_inverse_mixed_workspace_size(int64_t S) {
+    Sizer s;
+    s.take<float>(2 * S * S);  // A planes
+    s.take<float>(2 * S * S);  // A^-1 planes
+    s.take<char>(dfspd_bytes(S, true));
+    return s.total();
+}
+
+int aj_spd_inverse_mixed(const double* A, int64_t S, double* Ainv, double* logdet, void* workspace,
+                         size_t workspace_bytes, int* info, void* stream) {
+    if (S < 0) return AJ_ERR_ARG;
+    if (S == 0) return AJ_OK;
+    if (!A || !Ainv) return AJ_ERR_ARG;
+    if (!workspace || workspace_bytes < aj_spd_inverse_mixed_workspace_size(S)) return AJ_ERR_WORKSPACE;
+    cudaStream_t st = as_stream(stream);
+    Carver cv(workspace, workspace_bytes);
+    float* Ap = cv.take<float>(2 * S * S);
+    float* Ip = cv.take<float>(2 * S * S);
+    char* sub = cv.take<char>(dfspd_bytes(S, true));
+    Carver sc(sub, dfspd_bytes(S, true));
+    DfSpd w = dfspd_carve(sc, S, true);
+    AJ_TRY(df_split(A, S * S, Ap, Ap + S * S, st));
+    AJ_TRY(dfspd_factor(Ap, Ap + S * S, S, w, logdet, info, st));
+    AJ_TRY(dfspd_invert_factor(S, w, st));
+    AJ_TRY(dfspd_inverse_from_factor(S, w, Ip, Ip + S * S, st));
+    return df_join(Ip, Ip + S * S, S * S, Ainv, st);
+}
+
+}  // extern "C"

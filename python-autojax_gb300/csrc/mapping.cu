@@ -169,7 +169,8 @@ __global__ void csc_offsets_kernel(const int* __restrict__ hist, int64_t nchunk,
 // 32-entry group are ranked with a match mask so writes stay in (m, b) order
 __global__ void csc_place_kernel(const int64_t* __restrict__ idx, const double* __restrict__ w,
                                  const int64_t* __restrict__ sizes, int64_t M, int64_t B, int64_t S, CscMode mode,
-                                 int* __restrict__ off, int* __restrict__ rows, double* __restrict__ vals) {
+                                 int* __restrict__ off, int* __restrict__ rows, double* __restrict__ vals,
+                                 float2* __restrict__ vdf) {
     const int64_t c = blockIdx.x;
     const int lane = threadIdx.x;
     const int64_t e0 = c * CSC_CHUNK, e1 = min(M * B, e0 + CSC_CHUNK);
@@ -186,8 +187,11 @@ __global__ void csc_place_kernel(const int64_t* __restrict__ idx, const double* 
         if (ok && lane == leader) basepos = cur[s];
         basepos = __shfl_sync(0xffffffffu, basepos, leader);
         if (ok) {
+            const double v = w[e];
+            const df d = df_from(v);
             rows[basepos + rank] = static_cast<int>(e / B);
-            vals[basepos + rank] = w[e];
+            vals[basepos + rank] = v;
+            vdf[basepos + rank] = make_float2(d.hi, d.lo);
         }
         __syncwarp();
         if (ok && lane == leader) cur[s] = basepos + __popc(peers);
@@ -226,7 +230,7 @@ __global__ void __launch_bounds__(256)
 // float4 fast path of the hot W T product: X rows 16-byte aligned, cols % 4 == 0
 __global__ void __launch_bounds__(256)
     csc_spmm_t_f32x4_kernel(const int* __restrict__ colptr, const int* __restrict__ rows,
-                            const double* __restrict__ vals, const float* __restrict__ X, int64_t ld_x, int64_t cols,
+                            const float2* __restrict__ vdf, const float* __restrict__ X, int64_t ld_x, int64_t cols,
                             float* __restrict__ out, int64_t ld_out) {
     const int64_t s = blockIdx.x;
     const int64_t c0 = (blockIdx.y * (int64_t)blockDim.x + threadIdx.x) * 4;
@@ -235,7 +239,7 @@ __global__ void __launch_bounds__(256)
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int q = b; q < e; ++q) {
         const float4 x = __ldg(reinterpret_cast<const float4*>(X + (int64_t)rows[q] * ld_x + c0));
-        const float a = static_cast<float>(vals[q]);
+        const float a = vdf[q].x;
         acc.x = fmaf(a, x.x, acc.x);
         acc.y = fmaf(a, x.y, acc.y);
         acc.z = fmaf(a, x.z, acc.z);
@@ -248,7 +252,7 @@ __global__ void __launch_bounds__(256)
 // float4 path below is used when rows are 16-byte aligned)
 template <bool VEC>
 __global__ void __launch_bounds__(256)
-    csc_spmm_t_df_kernel(const int* __restrict__ colptr, const int* __restrict__ rows, const double* __restrict__ vals,
+    csc_spmm_t_df_kernel(const int* __restrict__ colptr, const int* __restrict__ rows, const float2* __restrict__ vdf,
                          const float* __restrict__ Xh, const float* __restrict__ Xl, int64_t ld_x, int64_t cols,
                          float* __restrict__ Oh, float* __restrict__ Ol, int64_t ld_out) {
     const int64_t s = blockIdx.x;
@@ -267,7 +271,8 @@ __global__ void __launch_bounds__(256)
                 const int64_t off = (int64_t)rows[q + u] * ld_x + c0;
                 h[u] = __ldg(reinterpret_cast<const float4*>(Xh + off));
                 l[u] = __ldg(reinterpret_cast<const float4*>(Xl + off));
-                a[u] = df_from(vals[q + u]);
+                const float2 w = vdf[q + u];
+                a[u] = {w.x, w.y};
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
@@ -279,7 +284,8 @@ __global__ void __launch_bounds__(256)
         }
     }
     for (; q < e; ++q) {
-        const df a = df_from(vals[q]);
+        const float2 w = vdf[q];
+        const df a = {w.x, w.y};
         const int64_t off = (int64_t)rows[q] * ld_x + c0;
         if (VEC) {
             const float4 h = __ldg(reinterpret_cast<const float4*>(Xh + off));
@@ -425,6 +431,7 @@ size_t csc_bytes(int64_t M, int64_t B, int64_t S) {
     s.take<int>(S + 1);
     s.take<int>(M * B);
     s.take<double>(M * B);
+    s.take<float2>(M * B);
     s.take<int>(nch * S);  // hist
     s.take<int>(nch * S);  // offsets / cursors
     return s.total();
@@ -435,6 +442,7 @@ void csc_take(Carver& cv, int64_t M, int64_t B, int64_t S, Csc& c) {
     c.colptr = cv.take<int>(S + 1);
     c.rows = cv.take<int>(M * B);
     c.vals = cv.take<double>(M * B);
+    c.vdf = cv.take<float2>(M * B);
     c.keys = cv.take<int>(nch * S);
     c.cursor = cv.take<int>(nch * S);
 }
@@ -450,7 +458,7 @@ int csc_build(const int64_t* idx, const double* w, const int64_t* sizes, int64_t
     AJ_LAUNCHED();
     csc_offsets_kernel<<<1, 1024, 0, st>>>(hist, nch, S, c.colptr, off);
     AJ_LAUNCHED();
-    csc_place_kernel<<<(unsigned)nch, 32, 0, st>>>(idx, w, sizes, M, B, S, mode, off, c.rows, c.vals);
+    csc_place_kernel<<<(unsigned)nch, 32, 0, st>>>(idx, w, sizes, M, B, S, mode, off, c.rows, c.vals, c.vdf);
     return check_launch();
 }
 
@@ -463,7 +471,7 @@ int csc_spmm_t(const Csc& c, int64_t S, const Tin* X, int64_t ld_x, int64_t cols
                              (reinterpret_cast<uintptr_t>(X) % 16 == 0) && (reinterpret_cast<uintptr_t>(out) % 16 == 0);
         if (aligned) {
             dim3 grid((unsigned)S, (unsigned)((cols / 4 + 255) / 256));
-            csc_spmm_t_f32x4_kernel<<<grid, 256, 0, st>>>(c.colptr, c.rows, c.vals, X, ld_x, cols, out, ld_out);
+            csc_spmm_t_f32x4_kernel<<<grid, 256, 0, st>>>(c.colptr, c.rows, c.vdf, X, ld_x, cols, out, ld_out);
             return check_launch();
         }
     }
@@ -487,9 +495,9 @@ int csc_spmm_t_df(const Csc& c, int64_t S, const float* Xh, const float* Xl, int
     const bool vec = (cols % 4 == 0) && (ld_x % 4 == 0) && (reinterpret_cast<uintptr_t>(Xh) % 16 == 0) &&
                      (reinterpret_cast<uintptr_t>(Xl) % 16 == 0);
     if (vec)
-        csc_spmm_t_df_kernel<true><<<grid, 256, 0, st>>>(c.colptr, c.rows, c.vals, Xh, Xl, ld_x, cols, Oh, Ol, ld_out);
+        csc_spmm_t_df_kernel<true><<<grid, 256, 0, st>>>(c.colptr, c.rows, c.vdf, Xh, Xl, ld_x, cols, Oh, Ol, ld_out);
     else
-        csc_spmm_t_df_kernel<false><<<grid, 256, 0, st>>>(c.colptr, c.rows, c.vals, Xh, Xl, ld_x, cols, Oh, Ol, ld_out);
+        csc_spmm_t_df_kernel<false><<<grid, 256, 0, st>>>(c.colptr, c.rows, c.vdf, Xh, Xl, ld_x, cols, Oh, Ol, ld_out);
     return check_launch();
 }
 

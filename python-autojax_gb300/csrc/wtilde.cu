@@ -8,9 +8,13 @@
 // argument reduction t - rint(t) in float64; the product then costs 2 fused
 // multiply-adds per (pixel pair, visibility) instead of one cos per pair.
 //   AJ_FP64 : float64 panel and float64 tiles (parity path).
-//   AJ_MIXED: float32 sincospi of the float64-reduced phase; 128x128 float32
-//             tiles whose register sums are Kahan-folded into shared memory
-//             every FOLD k-rows and added into the float64 result per chunk.
+//   AJ_MIXED: float64 sincospi panel split into double-float (hi, lo) float32
+//             planes; the product runs in double-float on the float32 pipe
+//             (gemm_df, lower tiles, accumulated over K chunks) and yields
+//             the double-float planes the mixed likelihood reads.  (A float32
+//             panel, even with exactly summed products, moves logE by 1-5e-6
+//             at the benchmark's conditioning, so no float32 rounding of the
+//             panel values is allowed.)
 // Only lower-triangular tiles are computed; each writes its mirror too.
 //
 // Compact table (numba.py:211-234).  With a = D n1 u, b = D n0 v the same
@@ -23,7 +27,7 @@
 
 #include <math.h>
 
-#include "aj_common.cuh"
+#include "aj_internal.cuh"
 
 namespace aj {
 
@@ -78,109 +82,6 @@ __device__ __forceinline__ void lower_tile(int64_t t, int64_t& bi, int64_t& bj) 
     bj = t - r * (r + 1) / 2;
 }
 
-// ---------------------------------------------- float32 SYRK with Kahan fold
-
-// C64 (+)= P^T P restricted to the lower tile (bi, bj), mirrored.
-// P: kd x Mp float32, k-major; kd a multiple of SLAB; Mp a multiple of 128.
-__global__ void __launch_bounds__(256, 1)
-    syrk_f32_kahan_kernel(const float* __restrict__ P, int64_t Mp, int64_t kd, int64_t M, double* __restrict__ C,
-                          int accumulate) {
-    extern __shared__ float smem[];
-    float* As = smem;                    // [2][SLAB][128]
-    float* Bs = As + 2 * SLAB * 128;     // [2][SLAB][128]
-    float* hi = Bs + 2 * SLAB * 128;     // [64][256]
-    float* lo = hi + 64 * 256;           // [64][256]
-
-    int64_t bi, bj;
-    lower_tile(blockIdx.x, bi, bj);
-    const int64_t a0 = bi * 128, b0 = bj * 128;
-    const int tid = threadIdx.x;
-    const int tx = tid & 15, ty = tid >> 4;
-    const int lrow = tid >> 5, lcol = (tid & 31) * 4;
-
-    float acc[8][8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-#pragma unroll
-        for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-#pragma unroll 8
-    for (int q = 0; q < 64; ++q) {
-        hi[q * 256 + tid] = 0.f;
-        lo[q * 256 + tid] = 0.f;
-    }
-
-    const float* pa = P + a0 + lcol;
-    const float* pb = P + b0 + lcol;
-    float4 ra = *reinterpret_cast<const float4*>(pa + (int64_t)lrow * Mp);
-    float4 rb = *reinterpret_cast<const float4*>(pb + (int64_t)lrow * Mp);
-    *reinterpret_cast<float4*>(&As[lrow * 128 + lcol]) = ra;
-    *reinterpret_cast<float4*>(&Bs[lrow * 128 + lcol]) = rb;
-    __syncthreads();
-
-    const int64_t nslab = kd / SLAB;
-    int buf = 0;
-    for (int64_t sl = 0; sl < nslab; ++sl) {
-        const bool more = sl + 1 < nslab;
-        if (more) {
-            const int64_t kr = (sl + 1) * SLAB + lrow;
-            ra = __ldg(reinterpret_cast<const float4*>(pa + kr * Mp));
-            rb = __ldg(reinterpret_cast<const float4*>(pb + kr * Mp));
-        }
-        const float* as = As + buf * SLAB * 128;
-        const float* bs = Bs + buf * SLAB * 128;
-#pragma unroll
-        for (int kk = 0; kk < SLAB; ++kk) {
-            const float4 x0 = *reinterpret_cast<const float4*>(&as[kk * 128 + ty * 4]);
-            const float4 x1 = *reinterpret_cast<const float4*>(&as[kk * 128 + 64 + ty * 4]);
-            const float4 y0 = *reinterpret_cast<const float4*>(&bs[kk * 128 + tx * 4]);
-            const float4 y1 = *reinterpret_cast<const float4*>(&bs[kk * 128 + 64 + tx * 4]);
-            const float a[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
-            const float b[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-#pragma unroll
-                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-        }
-        if (((sl + 1) * SLAB) % FOLD == 0 || !more) {
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    const int q = (i * 8 + j) * 256 + tid;
-                    float h = hi[q], l = lo[q];
-                    kahan_add(h, l, acc[i][j]);
-                    hi[q] = h;
-                    lo[q] = l;
-                    acc[i][j] = 0.f;
-                }
-        }
-        if (more) {
-            float* an = As + (buf ^ 1) * SLAB * 128;
-            float* bn = Bs + (buf ^ 1) * SLAB * 128;
-            *reinterpret_cast<float4*>(&an[lrow * 128 + lcol]) = ra;
-            *reinterpret_cast<float4*>(&bn[lrow * 128 + lcol]) = rb;
-        }
-        __syncthreads();
-        buf ^= 1;
-    }
-
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        const int64_t gi = a0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int64_t gj = b0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
-            if (gi < M && gj < M) {
-                const int q = (i * 8 + j) * 256 + tid;
-                double v = (double)hi[q] - (double)lo[q];
-                if (accumulate) v += C[gi * M + gj];
-                C[gi * M + gj] = v;
-                if (bi != bj) C[gj * M + gi] = v;
-            }
-        }
-    }
-}
-
 // ---------------------------------------------------------- float64 SYRK
 
 // C (+)= P^T P on lower 64x64 tiles, mirrored. P: kd x Mp float64.
@@ -232,9 +133,29 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-__global__ void f64_to_f32_kernel(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
-        b[t] = static_cast<float>(a[t]);
+// Double-float panel: float64 sincospi of the phase, scaled by sqrt(w), split into hi/lo planes.
+__global__ void wtilde_panel_df_kernel(const double* __restrict__ sigma, const double* __restrict__ uv,
+                                       const double* __restrict__ grid, int64_t K, int64_t M, int64_t k0, int64_t kc,
+                                       int64_t Mp, float* __restrict__ Ph, float* __restrict__ Pl) {
+    const int64_t kk = blockIdx.x;
+    const int64_t i = blockIdx.y * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= Mp) return;
+    const int64_t k = k0 + kk;
+    double c = 0.0, s = 0.0;
+    if (k < K && i < M) {
+        const double u = uv[2 * k], v = uv[2 * k + 1];
+        const double t = fma(grid[2 * i + 1], u, grid[2 * i] * v);
+        const double sw = 1.0 / fabs(sigma[k]);
+        double sd, cd;
+        sincospi(2.0 * t, &sd, &cd);
+        c = cd * sw;
+        s = sd * sw;
+    }
+    const float ch = __double2float_rn(c), sh = __double2float_rn(s);
+    Ph[kk * Mp + i] = ch;
+    Pl[kk * Mp + i] = __double2float_rn(c - (double)ch);
+    Ph[(kc + kk) * Mp + i] = sh;
+    Pl[(kc + kk) * Mp + i] = __double2float_rn(s - (double)sh);
 }
 
 // --------------------------------------------------------------- compact
@@ -523,7 +444,7 @@ struct WtildePlan {
 WtildePlan wtilde_plan(int64_t K, int64_t M, int precision) {
     WtildePlan p;
     p.Mp = pad_to(M > 0 ? M : 1, PANEL_ROW_PAD);
-    p.elem = precision == AJ_MIXED ? 4 : 8;
+    p.elem = 8;  // float64, or a hi + lo pair of float32
     int64_t kc = (int64_t)(PANEL_BUDGET / (2 * p.Mp * p.elem));
     kc = kc / 64 * 64;
     if (kc < 64) kc = 64;
@@ -540,9 +461,10 @@ struct CompactPlan {
 };
 
 CompactPlan compact_plan(int64_t N, int64_t K, int precision) {
+    (void)precision;  // the compact table always runs the float64 kernels (~30 ms at K = 1e6)
     CompactPlan p;
     p.Np = pad_to(N > 0 ? N : 1, 64);
-    p.elem = precision == AJ_MIXED ? 4 : 8;
+    p.elem = 8;
     int64_t kc = (int64_t)((size_t(256) << 20) / (4 * p.Np * p.elem));
     kc = kc / 64 * 64;
     if (kc < 64) kc = 64;
@@ -599,58 +521,74 @@ extern "C" {
 
 size_t aj_w_tilde_curvature_workspace_size(int64_t K, int64_t M, int precision) {
     WtildePlan p = wtilde_plan(K, M, precision);
+    size_t panel = 2 * p.kc * p.Mp * p.elem;
+    // the mixed path may join its double-float planes through this buffer
+    if (precision == AJ_MIXED && panel < sizeof(double) * M * M) panel = sizeof(double) * M * M;
     Sizer s;
-    s.take<char>(2 * p.kc * p.Mp * p.elem);
+    s.take<char>(panel);
     return s.total();
 }
 
 int aj_w_tilde_curvature(const double* noise_map_real, const double* uv, const double* grid_slim, int64_t K,
-                         int64_t M, double* out64, float* out32, void* workspace, size_t workspace_bytes,
+                         int64_t M, double* out64, float* out_planes, void* workspace, size_t workspace_bytes,
                          int precision, void* stream) {
     if (K < 0 || M < 0 || (precision != AJ_FP64 && precision != AJ_MIXED)) return AJ_ERR_ARG;
     if (M == 0) return AJ_OK;
     if (!out64 || !grid_slim || (K > 0 && (!noise_map_real || !uv))) return AJ_ERR_ARG;
     cudaStream_t st = as_stream(stream);
+    float* ph = out_planes;
+    float* pl = out_planes ? out_planes + M * M : nullptr;
     if (K == 0) {
         if (cudaMemsetAsync(out64, 0, sizeof(double) * M * M, st) != cudaSuccess) return AJ_ERR_CUDA;
-        if (out32 && cudaMemsetAsync(out32, 0, sizeof(float) * M * M, st) != cudaSuccess) return AJ_ERR_CUDA;
+        if (out_planes && cudaMemsetAsync(out_planes, 0, sizeof(float) * 2 * M * M, st) != cudaSuccess)
+            return AJ_ERR_CUDA;
         return AJ_OK;
     }
     WtildePlan p = wtilde_plan(K, M, precision);
     if (workspace_bytes < aj_w_tilde_curvature_workspace_size(K, M, precision) || !workspace) return AJ_ERR_WORKSPACE;
-    const int64_t nt = p.Mp / (precision == AJ_MIXED ? 128 : 64);
-    const int64_t ntiles = nt * (nt + 1) / 2;
-    static bool attr_set[64] = {false};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    const size_t smem32 = (size_t)(4 * SLAB * 128 + 2 * 64 * 256) * sizeof(float);
-    if (precision == AJ_MIXED && dev < 64 && !attr_set[dev]) {
-        if (cudaFuncSetAttribute(syrk_f32_kahan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32) !=
-            cudaSuccess)
-            return AJ_ERR_CUDA;
-        attr_set[dev] = true;
+    if (precision == AJ_MIXED) {
+        // the double-float result accumulates in planes: the caller's, else the float64 output's bytes
+        const bool own = out_planes == nullptr;
+        if (own) {
+            ph = reinterpret_cast<float*>(out64);
+            pl = ph + M * M;  // out64 holds exactly 2 M^2 floats
+        }
+        float* Ph = static_cast<float*>(workspace);
+        float* Pl = Ph + 2 * p.kc * p.Mp;
+        for (int64_t ch = 0; ch < p.nchunk; ++ch) {
+            const int64_t k0 = ch * p.kc;
+            dim3 pg((unsigned)p.kc, (unsigned)((p.Mp + 255) / 256));
+            wtilde_panel_df_kernel<<<pg, 256, 0, st>>>(noise_map_real, uv, grid_slim, K, M, k0, p.kc, p.Mp, Ph, Pl);
+            AJ_LAUNCHED();
+            // W (+)= P^T P on lower 64x64 tiles
+            AJ_TRY(gemm_df(true, false, M, M, 2 * p.kc, false, Ph, Pl, p.Mp, Ph, Pl, p.Mp, ch > 0, ph, pl, M, true,
+                           false, st));
+        }
+        AJ_TRY(df_mirror_lower(ph, pl, M, st));
+        if (own) {
+            // planes live in out64's storage: join in place from the back is unsafe, so join via the panel buffer
+            // the workspace holds at least M^2 doubles for this join (see the size function)
+            double* tmp = reinterpret_cast<double*>(workspace);
+            AJ_TRY(df_join(ph, pl, M * M, tmp, st));
+            if (cudaMemcpyAsync(out64, tmp, sizeof(double) * M * M, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+                return AJ_ERR_CUDA;
+        } else {
+            AJ_TRY(df_join(ph, pl, M * M, out64, st));
+        }
+        return AJ_OK;
     }
+    const int64_t nt = p.Mp / 64;
+    const int64_t ntiles = nt * (nt + 1) / 2;
     for (int64_t ch = 0; ch < p.nchunk; ++ch) {
         const int64_t k0 = ch * p.kc;
         dim3 pg((unsigned)p.kc, (unsigned)((p.Mp + 255) / 256));
-        if (precision == AJ_MIXED) {
-            float* P = static_cast<float*>(workspace);
-            wtilde_panel_kernel<float><<<pg, 256, 0, st>>>(noise_map_real, uv, grid_slim, K, M, k0, p.kc, p.Mp, P);
-            AJ_LAUNCHED();
-            syrk_f32_kahan_kernel<<<(unsigned)ntiles, 256, smem32, st>>>(P, p.Mp, 2 * p.kc, M, out64, ch > 0);
-            AJ_LAUNCHED();
-        } else {
-            double* P = static_cast<double*>(workspace);
-            wtilde_panel_kernel<double><<<pg, 256, 0, st>>>(noise_map_real, uv, grid_slim, K, M, k0, p.kc, p.Mp, P);
-            AJ_LAUNCHED();
-            syrk_f64_kernel<<<(unsigned)ntiles, 256, 0, st>>>(P, p.Mp, 2 * p.kc, M, out64, ch > 0);
-            AJ_LAUNCHED();
-        }
-    }
-    if (out32) {
-        f64_to_f32_kernel<<<blocks_for(M * M, 256, 8 * num_sms()), 256, 0, st>>>(out64, out32, M * M);
+        double* P = static_cast<double*>(workspace);
+        wtilde_panel_kernel<double><<<pg, 256, 0, st>>>(noise_map_real, uv, grid_slim, K, M, k0, p.kc, p.Mp, P);
+        AJ_LAUNCHED();
+        syrk_f64_kernel<<<(unsigned)ntiles, 256, 0, st>>>(P, p.Mp, 2 * p.kc, M, out64, ch > 0);
         AJ_LAUNCHED();
     }
+    if (out_planes) AJ_TRY(df_split(out64, M * M, ph, pl, st));
     return AJ_OK;
 }
 
@@ -684,19 +622,11 @@ int aj_w_compact_curvature(int64_t N, const double* noise_map_real, const double
         const int64_t k0 = ch * p.kc;
         dim3 pg((unsigned)p.kc, (unsigned)((p.Np + 127) / 128));
         dim3 gg((unsigned)ntile, (unsigned)p.nsplit, 2);
-        if (precision == AJ_MIXED) {
-            compact_panel_kernel<float><<<pg, 128, 0, st>>>(noise_map_real, uv, K, N, p.Np, ps_rad, k0, p.kc,
-                                                            reinterpret_cast<float*>(tab));
-            AJ_LAUNCHED();
-            compact_gemm_kernel<float><<<gg, 256, 0, st>>>(reinterpret_cast<float*>(tab), p.kc, p.Np, p.k_per_split,
-                                                           partial);
-        } else {
-            compact_panel_kernel<double><<<pg, 128, 0, st>>>(noise_map_real, uv, K, N, p.Np, ps_rad, k0, p.kc,
-                                                             reinterpret_cast<double*>(tab));
-            AJ_LAUNCHED();
-            compact_gemm_kernel<double><<<gg, 256, 0, st>>>(reinterpret_cast<double*>(tab), p.kc, p.Np,
-                                                            p.k_per_split, partial);
-        }
+        compact_panel_kernel<double><<<pg, 128, 0, st>>>(noise_map_real, uv, K, N, p.Np, ps_rad, k0, p.kc,
+                                                         reinterpret_cast<double*>(tab));
+        AJ_LAUNCHED();
+        compact_gemm_kernel<double><<<gg, 256, 0, st>>>(reinterpret_cast<double*>(tab), p.kc, p.Np, p.k_per_split,
+                                                        partial);
         AJ_LAUNCHED();
         compact_reduce_kernel<<<blocks_for(2 * p.Np * p.Np, 256, 1024), 256, 0, st>>>(partial, p.nsplit, p.Np, accum,
                                                                                    ch == 0);

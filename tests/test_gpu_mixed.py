@@ -95,3 +95,19 @@ def test_autograd_function(aj):
     assert abs(float(out) - r[0]) <= 1e-10 * abs(r[0])
     np.testing.assert_allclose(w.grad.cpu().numpy(), r[2], rtol=1e-8, atol=1e-9 * np.abs(r[2]).max())
     assert abs(float(c.grad) - 2 * 1.3 * r[1]) <= 1e-7 * max(1.0, abs(2 * 1.3 * r[1]))
+
+
+@pytest.mark.parametrize("M,K", [(33, 65), (448, 2000), (300, 7)])
+def test_mixed_w_tilde_matches_oracle(aj, M, K):
+    """The double-float w_tilde build: float64 panel, double-float product (~1e-13 relative)."""
+    from oracle import numpy_port as ref
+
+    rng = np.random.default_rng(M + K)
+    g = rng.standard_normal((M, 2)) * 1e-5
+    uv = rng.uniform(-5e5, 5e5, (K, 2))
+    n = rng.uniform(0.1, 1.0, K)
+    W, P = aj.w_tilde_curvature_interferometer_from(n, uv, g, precision="mixed", planes=True)
+    exp = ref.w_tilde_curvature_interferometer_from(n, uv, g)
+    scale = np.abs(exp).max()
+    np.testing.assert_allclose(W, exp, rtol=0, atol=1e-12 * scale)
+    np.testing.assert_allclose(P[0].astype(np.float64) + P[1].astype(np.float64), W, rtol=0, atol=1e-15 * scale)
