@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
     ap.add_argument("--skip-wtilde", action="store_true", help="omit the w_tilde kernel measurement")
     ap.add_argument("--stages", action="store_true", help="also time the pipeline stages separately")
+    ap.add_argument("--skip-batch", action="store_true", help="omit the batched many-model measurement")
+    ap.add_argument("--batch", type=int, default=64, help="lens models in the batched measurement")
     return ap.parse_args()
 
 
@@ -386,7 +388,71 @@ def gpu_arm(args, dist: Dist) -> dict:
         result["w_tilde"] = wtilde_bench(d, dev, fp32_peak)
     if args.stages:
         result["stages_ms"] = stage_times(d, w_tilde, dev, dist)
+    if not args.skip_batch:
+        del ev, A, F, Ainv, ws_m, ws_f, w_tilde, w_compact
+        torch.cuda.empty_cache()
+        result["batched"] = batched_bench(args, dev, dist)
     return result
+
+
+def batched_bench(args, dev, dist: Dist) -> dict:
+    """Many lens models against one dataset (the batched configuration).
+
+    K = 500,000 visibilities, a 100 x 100 grid at 0.04" with a 2.0" mask
+    (~8,000 image pixels), ``--batch`` lens models with S uniform in
+    [500, 2000], Einstein radius uniform in [0.6", 1.2"] and lambda
+    log-uniform in [1e-3, 1e3]; mixed precision with gradients.  One step is
+    one replay of the captured batch graph (every model evaluated once);
+    ``sequential`` replays the models' own single-evaluation graphs one after
+    another on the same inputs.
+    """
+    import torch
+
+    import autojax_gb300 as aj
+    from autojax_gb300 import synthetic
+    from autojax_gb300.inversion import Dataset, LogEvidenceBatch
+
+    d = dataset("cfg5")
+    noise_real = torch.from_numpy(d["noise_map_real"]).to(dev)
+    uv = torch.from_numpy(d["uv_wavelengths"]).to(dev)
+    w_compact = aj.w_compact_curvature_interferometer_from(d["grid_size"], noise_real, uv, d["pixel_scale"])
+    w_tilde = aj.w_tilde_via_compact_from(w_compact, torch.from_numpy(d["native_index_for_slim_index"]).to(dev))
+    ds = Dataset(d["dirty_image"], d["data"], d["noise_map"], w_tilde, precision="mixed", device=dev)
+    lm = synthetic.lens_models(d, args.batch, seed=55 + dist.rank)
+    P = max(m["neighbors"].shape[1] for m in lm)
+    batch = LogEvidenceBatch(ds, [m["S"] for m in lm], B=3, P=P)
+    for i, m in enumerate(lm):
+        batch.set_model(i, m["pix_indexes_for_sub_slim_index"], m["pix_weights_for_sub_slim_index"], m["neighbors"],
+                        m["neighbors_sizes"], m["coefficient"])
+    batch.capture()
+    for _ in range(max(2, args.warmup)):
+        batch.step()
+    torch.cuda.synchronize()
+    batch.check()
+    steps = 5
+    t = time_region(lambda i: batch.step(), steps, dist, "timed_batch")
+    batch.check()
+    for e in batch.evals:
+        e.capture()
+    for e in batch.evals:
+        e.step()
+    t_seq = time_region(lambda i: [e.step() for e in batch.evals], 1, dist, "timed_batch_sequential")
+    for e in batch.evals:
+        e.release_graph()
+    n = batch.n
+    Ss = [m["S"] for m in lm]
+    return {
+        "workload": f"cfg5: K={d['K']} visibilities, M={d['M']} image pixels (100x100 at 0.04\", r=2.0\"); "
+                    f"{n} lens models, S uniform in [500, 2000] (drawn {min(Ss)}..{max(Ss)}), Einstein radius "
+                    f"uniform in [0.6, 1.2]\", lambda log-uniform in [1e-3, 1e3]; mixed precision with gradients",
+        "value": steps * n * dist.world / t,
+        "unit": "evals/s",
+        "ms_per_batch": 1e3 * t / steps,
+        "sequential_value": n * dist.world / t_seq,
+        "batched_over_sequential": t_seq / (t / steps),
+        "launches_per_batch": batch.launches_per_batch,
+        "graph": True,
+    }
 
 
 def wtilde_bench(d, dev, fp32_peak) -> dict:

@@ -266,6 +266,33 @@ size_t aj_log_evidence_workspace_size(const aj_problem* p, int precision, int wi
 int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* out, double* grad_weights,
                     double* reconstruction, void* workspace, size_t workspace_bytes, int* info, void* stream);
 
+/* Batched log-evidence: n independent lens-model evaluations in one call (no
+ * reference counterpart; the reference evaluates one model per call of
+ * numba.py:761-857).  problems[i] usually share dirty_image, data, noise_map
+ * and w_tilde (or w_compact); S, mapping, neighbours and coefficient are per
+ * evaluation.  out is (n, 2) and info (n, 2); grad_weights[i] (M, B),
+ * reconstruction[i] (S_i,) (the array may be NULL) and workspaces[i], of at
+ * least aj_log_evidence_workspace_size(&problems[i], ...) bytes, are per
+ * evaluation.  The evaluations run as up to AJ_BATCH_BRANCHES concurrent
+ * branches forked from `stream` and joined back into it; every problem is
+ * validated before anything is enqueued. */
+#define AJ_BATCH_BRANCHES 16
+int aj_log_evidence_batched(const aj_problem* problems, int64_t n, int precision, int with_grad, double* out,
+                            double* const* grad_weights, double* const* reconstruction, void* const* workspaces,
+                            const size_t* workspace_bytes, int* info, void* stream);
+
+/* CUDA-graph capture of library calls (no reference counterpart: the
+ * reference evaluates eagerly).  Everything enqueued on `stream` between
+ * aj_graph_begin and aj_graph_end is recorded, including the work the library
+ * forks onto its own prioritised side streams, and instantiated so that
+ * replays keep those priorities.  `stream` must not be the legacy default
+ * stream.  Make one uncaptured call of the same work on the same stream
+ * first: the side streams are created then. */
+int aj_graph_begin(void* stream);
+int aj_graph_end(void* stream, void** graph_exec);
+int aj_graph_launch(void* graph_exec, void* stream);
+int aj_graph_destroy(void* graph_exec);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,6 +18,7 @@ AJ_ERR_CUDA = -2
 AJ_ERR_WORKSPACE = -3
 AJ_ERR_TOO_LARGE = -4
 AJ_NOALLOC_SOLVE_MAX_S = 1024
+AJ_BATCH_BRANCHES = 16
 AJ_INFO_INDEX_RANGE = 1
 AJ_INFO_NOT_POSITIVE_DEFINITE = 2
 AJ_FP64 = 0
@@ -100,6 +101,11 @@ SIGNATURES = {
     "aj_split_f64": (INT, [P, I64, P, P, P]),
     "aj_log_evidence_workspace_size": (SZ, [C.POINTER(Problem), INT, INT]),
     "aj_log_evidence": (INT, [C.POINTER(Problem), INT, INT, P, P, P, P, SZ, P, P]),
+    "aj_log_evidence_batched": (INT, [C.POINTER(Problem), I64, INT, INT, P, P, P, P, P, P, P]),
+    "aj_graph_begin": (INT, [P]),
+    "aj_graph_end": (INT, [P, C.POINTER(P)]),
+    "aj_graph_launch": (INT, [P, P]),
+    "aj_graph_destroy": (INT, [P]),
 }
 
 _lock = threading.Lock()

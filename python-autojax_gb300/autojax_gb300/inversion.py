@@ -13,6 +13,8 @@ gradients for the mapping weights and the regularisation coefficient.
 
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import torch
 
@@ -33,32 +35,30 @@ def _complex_real(x, device):
     return torch.from_numpy(a.view(np.float64).reshape(-1, 2)).to(device)
 
 
-class LogEvidence:
-    """Resident-dataset evaluator of the log-evidence and its gradient.
+class Dataset:
+    """The arrays every evaluation of one observation shares, resident on the device.
 
-    Parameters mirror ``log_likelihood_function_via_w_tilde_from``
-    (numba.py:761-857): pass ``w_tilde`` (M, M), or ``w_compact`` (N, 2N-1)
-    with ``native_index_for_slim_index`` for the compact form (numba.py:866-967).
-    Shapes of the per-model arrays (M x B mapping, S x P neighbours) are fixed
-    at construction by ``B``, ``S`` and ``P``.
+    The dirty image (M,), visibilities and noise (K,) complex128, and either
+    w_tilde (M, M) or the compact table w_compact (N, 2N-1) with
+    native_index_for_slim_index (M, 2), as the reference's likelihoods take
+    them (numba.py:761-857, 866-967).  For the mixed path the double-float
+    planes of w_tilde are split once here and reused by every evaluation.
     """
 
     def __init__(self, dirty_image, data, noise_map, w_tilde=None, *, w_compact=None, native_index_for_slim_index=None,
-                 S: int, B: int, P: int, precision: str = "mixed", with_grad: bool = True, device=None):
+                 precision: str = "mixed", device=None):
         if not torch.cuda.is_available():
-            raise RuntimeError("LogEvidence needs a CUDA device (autojax_gb300 has no CPU path)")
+            raise RuntimeError("autojax_gb300 needs a CUDA device (it has no CPU path)")
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         dev = self.device
         self.lib = _lib.load()
         self.precision = precision
         self.pc = precision_code(precision)
-        self.with_grad = bool(with_grad)
         self.dirty = _as_dev(dirty_image, torch.float64, dev)
         self.data = _complex_real(data, dev)
         self.noise = _complex_real(noise_map, dev)
         self.M = self.dirty.shape[0]
         self.K = self.data.shape[0]
-        self.S, self.B, self.P = int(S), int(B), int(P)
         self.w_tilde = _as_dev(w_tilde, torch.float64, dev) if w_tilde is not None else None
         self.w_compact = _as_dev(w_compact, torch.float64, dev) if w_compact is not None else None
         self.native = (_as_dev(native_index_for_slim_index, torch.int64, dev)
@@ -67,12 +67,58 @@ class LogEvidence:
             raise ValueError("pass w_tilde, or w_compact with native_index_for_slim_index")
         self.w_hi = self.w_lo = None
         if self.w_tilde is not None and self.pc == _lib.AJ_MIXED:
-            # double-float planes of w_tilde, split once for every evaluation
             self.w_hi = torch.empty(self.w_tilde.shape, dtype=torch.float32, device=dev)
             self.w_lo = torch.empty(self.w_tilde.shape, dtype=torch.float32, device=dev)
             _lib.check(self.lib.aj_split_f64(self.w_tilde.data_ptr(), self.w_tilde.numel(), self.w_hi.data_ptr(),
                                              self.w_lo.data_ptr(), torch.cuda.current_stream(dev).cuda_stream),
                        "aj_split_f64")
+
+    def fill(self, p: _lib.Problem) -> None:
+        """Set the shared fields of an aj_problem."""
+        p.M, p.K = self.M, self.K
+        p.dirty_image = self.dirty.data_ptr()
+        p.data = self.data.data_ptr()
+        p.noise_map = self.noise.data_ptr()
+        if self.w_tilde is not None:
+            p.w_tilde64 = self.w_tilde.data_ptr()
+            if self.w_hi is not None:
+                p.w_tilde_hi = self.w_hi.data_ptr()
+                p.w_tilde_lo = self.w_lo.data_ptr()
+        else:
+            p.w_compact = self.w_compact.data_ptr()
+            p.native_index = self.native.data_ptr()
+            p.N = self.w_compact.shape[0]
+
+
+class LogEvidence:
+    """Resident-dataset evaluator of the log-evidence and its gradient.
+
+    Parameters mirror ``log_likelihood_function_via_w_tilde_from``
+    (numba.py:761-857): pass ``w_tilde`` (M, M), or ``w_compact`` (N, 2N-1)
+    with ``native_index_for_slim_index`` for the compact form (numba.py:866-967).
+    Shapes of the per-model arrays (M x B mapping, S x P neighbours) are fixed
+    at construction by ``B``, ``S`` and ``P``.  Evaluators of several models
+    share one ``Dataset`` when it is passed as ``dataset`` (the other dataset
+    arguments are then omitted).
+    """
+
+    def __init__(self, dirty_image=None, data=None, noise_map=None, w_tilde=None, *, w_compact=None,
+                 native_index_for_slim_index=None, S: int, B: int, P: int, precision: str = "mixed",
+                 with_grad: bool = True, device=None, dataset: Dataset | None = None):
+        if dataset is None:
+            dataset = Dataset(dirty_image, data, noise_map, w_tilde, w_compact=w_compact,
+                              native_index_for_slim_index=native_index_for_slim_index, precision=precision,
+                              device=device)
+        elif precision_code(precision) != dataset.pc:
+            raise ValueError("precision differs from the dataset's")
+        self.dataset = ds = dataset
+        self.device = dev = ds.device
+        self.lib = ds.lib
+        self.precision = ds.precision
+        self.pc = ds.pc
+        self.with_grad = bool(with_grad)
+        self.M, self.K = ds.M, ds.K
+        self.S, self.B, self.P = int(S), int(B), int(P)
         # persistent per-model inputs (graph replays read these addresses)
         self.pix_indexes = torch.zeros((self.M, self.B), dtype=torch.int64, device=dev)
         self.pix_weights = torch.zeros((self.M, self.B), dtype=torch.float64, device=dev)
@@ -102,19 +148,8 @@ class LogEvidence:
 
     def _problem(self) -> _lib.Problem:
         p = _lib.Problem()
-        p.M, p.K, p.S, p.B, p.P = self.M, self.K, self.S, self.B, self.P
-        p.dirty_image = self.dirty.data_ptr()
-        p.data = self.data.data_ptr()
-        p.noise_map = self.noise.data_ptr()
-        if self.w_tilde is not None:
-            p.w_tilde64 = self.w_tilde.data_ptr()
-            if self.w_hi is not None:
-                p.w_tilde_hi = self.w_hi.data_ptr()
-                p.w_tilde_lo = self.w_lo.data_ptr()
-        else:
-            p.w_compact = self.w_compact.data_ptr()
-            p.native_index = self.native.data_ptr()
-            p.N = self.w_compact.shape[0]
+        self.dataset.fill(p)
+        p.S, p.B, p.P = self.S, self.B, self.P
         p.pix_indexes = self.pix_indexes.data_ptr()
         p.pix_weights = self.pix_weights.data_ptr()
         p.neighbors = self.neighbors.data_ptr()
@@ -154,21 +189,52 @@ class LogEvidence:
         _lib.check(rc, "aj_log_evidence")
 
     def capture(self):
-        """Record one evaluation into a CUDA graph (after a warm-up call); step() then replays it."""
-        self.launch()
+        """Record one evaluation into a CUDA graph (after a warm-up call); step() then replays it.
+
+        The capture goes through the library (aj_graph_begin/end) rather than
+        torch.cuda.graph: the library instantiates the graph so replays keep
+        the stream priorities of its factorisation lanes.  Nothing allocates
+        while capturing (all buffers exist already).
+        """
+        if self.graph is not None:
+            self.release_graph()
+        cap = torch.cuda.Stream(self.device)
+        cap.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(cap):
+            self.launch()  # warm-up on the capture stream: creates its side streams
         torch.cuda.synchronize(self.device)
         before = self.lib.aj_launch_count()
-        g = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(g):
-            self.launch()
+        _lib.check(self.lib.aj_graph_begin(cap.cuda_stream), "aj_graph_begin")
+        exec_ = ctypes.c_void_p()
+        try:
+            with torch.cuda.stream(cap):
+                self.launch()
+        except BaseException:
+            if self.lib.aj_graph_end(cap.cuda_stream, ctypes.byref(exec_)) == _lib.AJ_OK:
+                self.lib.aj_graph_destroy(exec_)
+            raise
+        _lib.check(self.lib.aj_graph_end(cap.cuda_stream, ctypes.byref(exec_)), "aj_graph_end")
         self.launches_per_eval = int(self.lib.aj_launch_count() - before)
-        self.graph = g
-        return g
+        self._capture_stream = cap
+        self.graph = exec_
+        return exec_
+
+    def release_graph(self):
+        if self.graph is not None:
+            self.lib.aj_graph_destroy(self.graph)
+            self.graph = None
+
+    def __del__(self):
+        try:
+            self.release_graph()
+        except Exception:
+            pass
 
     def step(self):
         """One evaluation: graph replay when captured, else a direct launch."""
         if self.graph is not None:
-            self.graph.replay()
+            _lib.check(self.lib.aj_graph_launch(self.graph, torch.cuda.current_stream(self.device).cuda_stream),
+                       "aj_graph_launch")
         else:
             self.launch()
 
@@ -214,6 +280,103 @@ class LogEvidence:
         return self._h_out.numel() * 8 + (self._h_grad.numel() * 8 if self.with_grad else 0)
 
 
+class LogEvidenceBatch:
+    """Many lens models against one ``Dataset``, evaluated by one call.
+
+    Each model has its own source-pixel count (``S_list``), mapping,
+    neighbours and coefficient; ``B`` and ``P`` bound the mapping and
+    neighbour widths of every model.  ``launch()`` enqueues all evaluations
+    through ``aj_log_evidence_batched`` as concurrent branches of the current
+    stream; ``capture()`` records that into one CUDA graph, so ``step()``
+    evaluates the whole batch with one graph launch.  Results: ``out`` (n, 2)
+    holds logE and dlogE/dlambda per model, ``evals[i].grad_weights`` the
+    weight gradients.
+    """
+
+    def __init__(self, dataset: Dataset, S_list, *, B: int, P: int, with_grad: bool = True):
+        self.dataset = dataset
+        self.lib = dataset.lib
+        self.device = dataset.device
+        self.with_grad = bool(with_grad)
+        self.evals = [LogEvidence(S=int(S), B=B, P=P, precision=dataset.precision, with_grad=with_grad,
+                                  dataset=dataset) for S in S_list]
+        n = self.n = len(self.evals)
+        self.out = torch.zeros((n, 2), dtype=torch.float64, device=self.device)
+        self.info = torch.zeros((n, 2), dtype=torch.int32, device=self.device)
+        self._problems = (_lib.Problem * n)(*[e.problem for e in self.evals])
+        self._grads = (ctypes.c_void_p * n)(*[e.grad_weights.data_ptr() for e in self.evals])
+        self._recons = (ctypes.c_void_p * n)(*[e.reconstruction.data_ptr() for e in self.evals])
+        self._ws = (ctypes.c_void_p * n)(*[e.workspace.data_ptr() for e in self.evals])
+        self._ws_bytes = (ctypes.c_size_t * n)(*[e.workspace.numel() for e in self.evals])
+        self.graph = None
+        self.launches_per_batch = None
+
+    def set_model(self, i, pix_indexes, pix_weights, neighbors, neighbors_sizes, coefficient=1.0):
+        self.evals[i].set_model(pix_indexes, pix_weights, neighbors, neighbors_sizes, coefficient)
+
+    def launch(self):
+        """Enqueue every evaluation on the current stream (no synchronisation)."""
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        self.info.zero_()
+        rc = self.lib.aj_log_evidence_batched(self._problems, self.n, self.dataset.pc, int(self.with_grad),
+                                              self.out.data_ptr(), ctypes.cast(self._grads, ctypes.c_void_p),
+                                              ctypes.cast(self._recons, ctypes.c_void_p),
+                                              ctypes.cast(self._ws, ctypes.c_void_p),
+                                              ctypes.cast(self._ws_bytes, ctypes.c_void_p), self.info.data_ptr(),
+                                              stream)
+        _lib.check(rc, "aj_log_evidence_batched")
+
+    def capture(self):
+        """Record one batch into a CUDA graph (after a warm-up call on the capture stream)."""
+        if self.graph is not None:
+            self.release_graph()
+        cap = torch.cuda.Stream(self.device)
+        cap.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(cap):
+            self.launch()
+        torch.cuda.synchronize(self.device)
+        before = self.lib.aj_launch_count()
+        exec_ = ctypes.c_void_p()
+        _lib.check(self.lib.aj_graph_begin(cap.cuda_stream), "aj_graph_begin")
+        try:
+            with torch.cuda.stream(cap):
+                self.launch()
+        except BaseException:
+            if self.lib.aj_graph_end(cap.cuda_stream, ctypes.byref(exec_)) == _lib.AJ_OK:
+                self.lib.aj_graph_destroy(exec_)
+            raise
+        _lib.check(self.lib.aj_graph_end(cap.cuda_stream, ctypes.byref(exec_)), "aj_graph_end")
+        self.launches_per_batch = int(self.lib.aj_launch_count() - before)
+        self._capture_stream = cap
+        self.graph = exec_
+        return exec_
+
+    def release_graph(self):
+        if self.graph is not None:
+            self.lib.aj_graph_destroy(self.graph)
+            self.graph = None
+
+    def __del__(self):
+        try:
+            self.release_graph()
+        except Exception:
+            pass
+
+    def step(self):
+        if self.graph is not None:
+            _lib.check(self.lib.aj_graph_launch(self.graph, torch.cuda.current_stream(self.device).cuda_stream),
+                       "aj_graph_launch")
+        else:
+            self.launch()
+
+    def check(self):
+        for i, (code, where) in enumerate(self.info.tolist()):
+            if code == _lib.AJ_INFO_NOT_POSITIVE_DEFINITE:
+                raise np.linalg.LinAlgError(f"model {i}: curvature_reg_matrix is not positive definite (pivot {where})")
+            if code == _lib.AJ_INFO_INDEX_RANGE:
+                raise IndexError(f"model {i}: index out of range (flat position {where})")
+
+
 class LogEvidenceFunction(torch.autograd.Function):
     """logE(pix_weights, coefficient) for a LogEvidence evaluator with its model indices set.
 
@@ -243,4 +406,4 @@ def log_evidence(pix_weights: torch.Tensor, coefficient: torch.Tensor, evaluator
     return LogEvidenceFunction.apply(pix_weights, coefficient, evaluator)
 
 
-__all__ = ["LogEvidence", "LogEvidenceFunction", "log_evidence", "PRECISIONS"]
+__all__ = ["Dataset", "LogEvidence", "LogEvidenceBatch", "LogEvidenceFunction", "log_evidence", "PRECISIONS"]

@@ -35,6 +35,23 @@ int spd_solve_vec(int64_t S, SpdWorkspace& w, const double* b, double* x, int* i
 // Ainv (S x S, full symmetric) = Linv^T Linv
 int spd_inverse_from_factor(int64_t S, SpdWorkspace& w, double* Ainv, cudaStream_t st);
 
+// ---- lanes.cu (side streams that fork from and join back into the caller's stream)
+
+constexpr int kLaneCount = 3;  // 0: critical chain (highest priority), 1: bulk updates, 2: triangular inverse
+enum LaneEvent { kEvFork = 0, kEvPanel, kEvUpdate, kEvDiag, kEvJoin0, kLaneEvents = kEvJoin0 + kLaneCount };
+struct Lanes {
+    cudaStream_t s[kLaneCount];
+    cudaEvent_t ev[kLaneEvents];
+};
+// the lanes that forks from `caller` use on the current device (created on first use)
+int lanes_for(cudaStream_t caller, Lanes** out);
+// lanes 0..n-1 start after the work already on st
+int lanes_fork(Lanes& l, cudaStream_t st, int n);
+// st continues after the work on lanes 0..n-1
+int lanes_join(Lanes& l, cudaStream_t st, int n);
+int lane_signal(Lanes& l, int event, int from);
+int lane_wait(Lanes& l, int lane, int event);
+
 // ---- linalg_df.cu (double-float planes: hi and lo float arrays)
 
 struct DfSpd {
@@ -54,11 +71,11 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
             const float* Bh, const float* Bl, int64_t ldb, bool accumulate, float* Ch, float* Cl, int64_t ldc,
             bool lower_only, bool tri_k, cudaStream_t st);
 int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* logdet, int* info, cudaStream_t st);
-int dfspd_invert_factor(int64_t S, DfSpd& w, cudaStream_t st);
-// the same for count = 1 or 2 independent matrices sharing every launch
-int dfspd_factor_n(const float* const* Ah, const float* const* Al, int count, int64_t S, DfSpd* const* w,
-                   double* const* logdet, int* info, cudaStream_t st);
-int dfspd_invert_factor_n(int64_t S, DfSpd* const* w, int count, cudaStream_t st);
+// The same for count = 1 or 2 independent matrices sharing every launch; the
+// first n_inverse of them also get their inverse factor L^-1 (in w->Ih/Il),
+// computed alongside the factorisation as its panels complete.
+int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int count, int n_inverse, int64_t S,
+                          DfSpd* const* w, double* const* logdet, int* info, cudaStream_t st);
 int dfspd_inverse_from_factor(int64_t S, DfSpd& w, float* Ah, float* Al, cudaStream_t st);
 int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st);
 int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x, double* r,

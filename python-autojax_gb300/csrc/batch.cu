@@ -1,0 +1,104 @@
+// Many lens-model evaluations against one dataset in a single call.
+//
+// An MCMC or nested sampler evaluates many lens models (each with its own
+// source-pixel count S, mapping, neighbours and regularisation coefficient)
+// against one observation: the dirty image, visibilities, noise and w_tilde
+// are shared and stay resident.  One evaluation is a chain of small,
+// latency-bound launches (the blocked factorisations); run alone it leaves
+// most of the GPU idle.  The batch therefore forks the caller's stream into
+// branch streams, enqueues the evaluations round-robin over the branches, and
+// joins them back, so the chains of different evaluations fill each other's
+// gaps.  Captured into one CUDA graph (aj_graph_begin/end), a whole batch is a
+// single graph launch whose branches the GPU runs concurrently.
+//
+// Branch streams are created once per (device, caller stream) on first use,
+// like the factorisation lanes, which are in turn keyed by branch stream, so
+// every evaluation in flight has its own lanes.
+
+#include <map>
+#include <mutex>
+
+#include "aj_internal.cuh"
+
+namespace aj {
+
+namespace {
+
+constexpr int kBranches = AJ_BATCH_BRANCHES;
+
+struct Branches {
+    cudaStream_t s[kBranches];
+    cudaEvent_t fork;
+    cudaEvent_t join[kBranches];
+};
+
+std::mutex g_branch_mu;
+std::map<std::pair<int, cudaStream_t>, Branches*> g_branches;
+
+int branches_for(cudaStream_t caller, Branches** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return AJ_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_branch_mu);
+    auto it = g_branches.find({dev, caller});
+    if (it == g_branches.end()) {
+        Branches* b = new Branches{};
+        bool ok = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+        for (int i = 0; ok && i < kBranches; ++i)
+            ok = cudaStreamCreateWithFlags(&b->s[i], cudaStreamNonBlocking) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming) == cudaSuccess;
+        if (!ok) {
+            g_last_cuda_error = static_cast<int>(cudaGetLastError());
+            delete b;  // handles created before the failure stay with the context
+            return AJ_ERR_CUDA;
+        }
+        it = g_branches.emplace(std::make_pair(dev, caller), b).first;
+    }
+    *out = it->second;
+    return AJ_OK;
+}
+
+}  // namespace
+
+}  // namespace aj
+
+using namespace aj;
+
+extern "C" {
+
+int aj_log_evidence_batched(const aj_problem* problems, int64_t n, int precision, int with_grad, double* out,
+                            double* const* grad_weights, double* const* reconstruction, void* const* workspaces,
+                            const size_t* workspace_bytes, int* info, void* stream) {
+    if (n < 0) return AJ_ERR_ARG;
+    if (n == 0) return AJ_OK;
+    if (!problems || !out || !workspaces || !workspace_bytes || !info) return AJ_ERR_ARG;
+    if (precision != AJ_FP64 && precision != AJ_MIXED) return AJ_ERR_ARG;
+    if (with_grad && !grad_weights) return AJ_ERR_ARG;
+    // every evaluation is validated before anything is enqueued
+    for (int64_t i = 0; i < n; ++i) {
+        const size_t need = aj_log_evidence_workspace_size(&problems[i], precision, with_grad);
+        if (need == 0) return AJ_ERR_ARG;
+        if (!workspaces[i] || workspace_bytes[i] < need) return AJ_ERR_WORKSPACE;
+        if (with_grad && !grad_weights[i]) return AJ_ERR_ARG;
+    }
+    cudaStream_t st = as_stream(stream);
+    Branches* br = nullptr;
+    AJ_TRY(branches_for(st, &br));
+    const int nb = n < kBranches ? static_cast<int>(n) : kBranches;
+    if (cudaEventRecord(br->fork, st) != cudaSuccess) return AJ_ERR_CUDA;
+    for (int b = 0; b < nb; ++b)
+        if (cudaStreamWaitEvent(br->s[b], br->fork, 0) != cudaSuccess) return AJ_ERR_CUDA;
+    int rc = AJ_OK;
+    for (int64_t i = 0; i < n && rc == AJ_OK; ++i)
+        rc = aj_log_evidence(&problems[i], precision, with_grad, out + 2 * i, with_grad ? grad_weights[i] : nullptr,
+                             reconstruction ? reconstruction[i] : nullptr, workspaces[i], workspace_bytes[i],
+                             info + 2 * i, br->s[i % nb]);
+    // join even after a failed enqueue, so the caller's stream never runs ahead of a branch
+    for (int b = 0; b < nb; ++b) {
+        if (cudaEventRecord(br->join[b], br->s[b]) != cudaSuccess ||
+            cudaStreamWaitEvent(st, br->join[b], 0) != cudaSuccess)
+            return AJ_ERR_CUDA;
+    }
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,85 @@
+// Side streams for work that forks from, and joins back into, the caller's stream.
+//
+// The blocked factorisations are chains of small, latency-bound launches.  They
+// run faster as three concurrent chains: the critical one (pivot panel, then
+// the next block column of the trailing update) on a high-priority stream, the
+// bulk of each trailing update on a low-priority one, and the triangular
+// inverse, which needs only finished panels, on a third.  Every fork starts
+// with an event recorded on the caller's stream and every join ends with the
+// caller's stream waiting on each lane, so the caller sees one ordered stream,
+// and stream capture records the same dependencies as graph edges.
+//
+// Streams and events are created once per (device, caller stream) on first
+// use and live until the process exits.  Keying by the caller's stream keeps
+// concurrent callers apart: evaluations enqueued on different streams (or
+// captured as parallel branches of one graph) each fork onto lanes of their
+// own, so their chains stay concurrent and never share an event.
+
+#include <map>
+#include <mutex>
+
+#include "aj_internal.cuh"
+
+namespace aj {
+
+namespace {
+
+std::mutex g_lanes_mu;
+std::map<std::pair<int, cudaStream_t>, Lanes*> g_lanes;
+
+int create_lanes(Lanes& l) {
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return AJ_ERR_CUDA;
+    const int prio[kLaneCount] = {greatest, least, greatest < least ? greatest + 1 : least};
+    for (int i = 0; i < kLaneCount; ++i)
+        if (cudaStreamCreateWithPriority(&l.s[i], cudaStreamNonBlocking, prio[i]) != cudaSuccess) return AJ_ERR_CUDA;
+    for (int i = 0; i < kLaneEvents; ++i)
+        if (cudaEventCreateWithFlags(&l.ev[i], cudaEventDisableTiming) != cudaSuccess) return AJ_ERR_CUDA;
+    return AJ_OK;
+}
+
+}  // namespace
+
+int lanes_for(cudaStream_t caller, Lanes** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return AJ_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_lanes_mu);
+    auto it = g_lanes.find({dev, caller});
+    if (it == g_lanes.end()) {
+        Lanes* l = new Lanes{};
+        const int rc = create_lanes(*l);
+        if (rc != AJ_OK) {
+            g_last_cuda_error = static_cast<int>(cudaGetLastError());
+            delete l;  // streams or events created before the failure stay with the context
+            return rc;
+        }
+        it = g_lanes.emplace(std::make_pair(dev, caller), l).first;
+    }
+    *out = it->second;
+    return AJ_OK;
+}
+
+int lanes_fork(Lanes& l, cudaStream_t st, int n) {
+    if (cudaEventRecord(l.ev[kEvFork], st) != cudaSuccess) return AJ_ERR_CUDA;
+    for (int i = 0; i < n; ++i)
+        if (cudaStreamWaitEvent(l.s[i], l.ev[kEvFork], 0) != cudaSuccess) return AJ_ERR_CUDA;
+    return AJ_OK;
+}
+
+int lanes_join(Lanes& l, cudaStream_t st, int n) {
+    for (int i = 0; i < n; ++i) {
+        if (cudaEventRecord(l.ev[kEvJoin0 + i], l.s[i]) != cudaSuccess) return AJ_ERR_CUDA;
+        if (cudaStreamWaitEvent(st, l.ev[kEvJoin0 + i], 0) != cudaSuccess) return AJ_ERR_CUDA;
+    }
+    return AJ_OK;
+}
+
+int lane_signal(Lanes& l, int event, int from) {
+    return cudaEventRecord(l.ev[event], l.s[from]) == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+int lane_wait(Lanes& l, int lane, int event) {
+    return cudaStreamWaitEvent(l.s[lane], l.ev[event], 0) == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+}  // namespace aj

@@ -446,8 +446,7 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         const float* fl[2] = {b.Al, b.Hl};
         DfSpd* fw[2] = {&b.da, &b.dh};
         double* ld[2] = {b.logdets + 0, b.logdets + 1};
-        AJ_TRY(dfspd_factor_n(fh, fl, 2, S, fw, ld, info, st));
-        AJ_TRY(dfspd_invert_factor_n(S, fw, with_grad ? 2 : 1, st));
+        AJ_TRY(dfspd_factor_invert_n(fh, fl, 2, with_grad ? 2 : 1, S, fw, ld, info, st));
         AJ_TRY(dfspd_solve_refined(S, b.da, b.Ah, b.Al, b.D, b.s, b.res, st));
     }
 

@@ -32,7 +32,15 @@ struct DfMats {
     float* dh[2];
     float* dl[2];
     double* piv[2];
+    int ninv;  // matrices z < ninv also get L^-1: the panel writes its diagonal block
 };
+
+// element z of a kernel-parameter pair without indexing it dynamically (which
+// would copy the parameter block to the stack)
+template <typename T>
+__device__ __forceinline__ T pick(T const (&a)[2], int z) {
+    return z ? a[1] : a[0];
+}
 
 __device__ __forceinline__ df dfmul(df a, df b) {
     const float p = a.hi * b.hi;
@@ -71,8 +79,10 @@ __device__ __forceinline__ df dfrsqrt(df d) {
     return df_norm({r, 0.5f * r * h});
 }
 
+// tile t of the lower triangle, row-major: (bi, bj) with bj <= bi.  The float
+// square root is exact enough for a first guess (t < 2^24); the loops fix it.
 __device__ __forceinline__ void lower_tile_df(int64_t t, int64_t& bi, int64_t& bj) {
-    int64_t r = static_cast<int64_t>((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    int64_t r = static_cast<int64_t>((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
     while (r * (r + 1) / 2 > t) --r;
     while ((r + 1) * (r + 2) / 2 <= t) ++r;
     bi = r;
@@ -277,28 +287,36 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 // block 0 stores L_kk, its inverse and the pivots; block b >= 1 replaces the
 // 64 panel rows k0 + 32 + 64 (b - 1) .. by A_rows L_kk^-T.
 // Latency matters more than work here (one launch per 32 columns sits on the
-// critical path): the pivot step fuses the column scaling into the rank-1
-// update (two barriers a column), and the inverse spreads each column's
-// substitution over 8 threads whose partial dot products meet in shuffles.
-__global__ void __launch_bounds__(256)
+// critical path), so the kernel keeps its barrier count and its per-warp
+// instruction count low:
+//  - factor: one barrier a column; every thread evaluates the pivot itself and
+//    the column scaling is fused into the rank-1 update;
+//  - inverse: recursive doubling, 5 levels of two small products each
+//    (inv [[A, 0], [B, C]] = [[A^-1, 0], [-C^-1 B A^-1, C^-1]]);
+//  - panel product: each warp owns two columns whose triangular dot-product
+//    lengths add to 33, so all lanes of a warp run the same loop.
+constexpr int PANEL_THREADS = 512;
+
+__global__ void __launch_bounds__(PANEL_THREADS)
     dfchol_panel_kernel(DfMats mats, int64_t S, int64_t k0, int* info) {
     const int z = blockIdx.y;
-    float* __restrict__ Lh = mats.Lh[z];
-    float* __restrict__ Ll = mats.Ll[z];
+    float* __restrict__ Lh = pick(mats.Lh, z);
+    float* __restrict__ Ll = pick(mats.Ll, z);
     const int64_t kb = k0 / DNB;
-    float* __restrict__ dh = mats.dh[z] + kb * DNB * DNB;
-    float* __restrict__ dl = mats.dl[z] + kb * DNB * DNB;
-    double* __restrict__ piv = mats.piv[z];
+    float* __restrict__ dh = pick(mats.dh, z) + kb * DNB * DNB;
+    float* __restrict__ dl = pick(mats.dl, z) + kb * DNB * DNB;
+    double* __restrict__ piv = pick(mats.piv, z);
     __shared__ float ah[DNB][DNB + 1], al[DNB][DNB + 1];
     __shared__ float ih[DNB][DNB + 1], il[DNB][DNB + 1];
     __shared__ float lh[DNB][DNB + 1], ll[DNB][DNB + 1];
     __shared__ float rh[DNB], rl[DNB];
+    __shared__ float th[DNB * DNB / 4], tl[DNB * DNB / 4];
     __shared__ float xh[64][DNB + 1], xl[64][DNB + 1];
     __shared__ int bad;
     const int tid = threadIdx.x;
     const int64_t nb = (S - k0) < DNB ? (S - k0) : DNB;
     if (tid == 0) bad = 0;
-    for (int e = tid; e < DNB * DNB; e += 256) {
+    for (int e = tid; e < DNB * DNB; e += PANEL_THREADS) {
         const int i = e / DNB, j = e % DNB;
         float vh, vl;
         if (i < nb && j < nb) {
@@ -319,7 +337,7 @@ __global__ void __launch_bounds__(256)
     // panel rows are loaded up front so their latency overlaps the factorisation
     const int64_t r0 = k0 + DNB + (int64_t)(blockIdx.x - 1) * 64;
     if (blockIdx.x > 0) {
-        for (int e = tid; e < 64 * DNB; e += 256) {
+        for (int e = tid; e < 64 * DNB; e += PANEL_THREADS) {
             const int i = e / DNB, j = e % DNB;
             const int64_t r = r0 + i;
             const bool in = r < S && j < nb;
@@ -328,7 +346,7 @@ __global__ void __launch_bounds__(256)
         }
     }
     __syncthreads();
-    const int ur = tid >> 3, uq = tid & 7;  // update: row ur, columns uq, uq+8, ...
+    const int ur = tid >> 4, uq = tid & 15;  // update: row ur, columns uq and uq + 16
     // one barrier a column: every thread evaluates the pivot itself; the scaled
     // column goes to L (lh/ll) so the update can keep reading the unscaled one
     for (int j = 0; j < DNB; ++j) {
@@ -357,7 +375,7 @@ __global__ void __launch_bounds__(256)
                 ll[ur][j] = lrj.lo;
             }
 #pragma unroll
-            for (int c = uq; c < DNB; c += 8)
+            for (int c = uq; c < DNB; c += 16)
                 if (c > j && c <= ur) {
                     const df lcj = dfmul({ah[c][j], al[c][j]}, rj);
                     df v = {ah[ur][c], al[ur][c]};
@@ -369,81 +387,125 @@ __global__ void __launch_bounds__(256)
     }
     __syncthreads();
     if (bad) return;
-    // inverse X = L^-1, row by row: X[i][c] = -r_i sum_{p=c}^{i-1} L[i][p] X[p][c]; thread (c, q)
-    // sums p = c + q, c + q + 8, ... and the 8 partials of a column meet in shuffles
-    const int c = tid >> 3, q = tid & 7;
+    // inverse X = L^-1 by recursive doubling: at level b the 32 / (2b) pairs of
+    // b x b diagonal blocks (A above C, B the block of L between them) get
+    // their off-diagonal block -C^-1 (B A^-1), through T = B A^-1 in th/tl
     if (tid < DNB) {
         ih[tid][tid] = rh[tid];
         il[tid][tid] = rl[tid];
     }
     __syncthreads();
-    for (int i = 1; i < DNB; ++i) {
-        df part = {0.f, 0.f};
-        if (c < i)
-            for (int p = c + q; p < i; p += 8) df_fma_acc(part, {lh[i][p], ll[i][p]}, {ih[p][c], il[p][c]});
-#pragma unroll
-        for (int o = 4; o > 0; o >>= 1) {
-            const df other = {__shfl_xor_sync(0xffffffffu, part.hi, o), __shfl_xor_sync(0xffffffffu, part.lo, o)};
-            part = df_add(part, other);
+    for (int b = 1; b < DNB; b <<= 1) {
+        const int n = (DNB / 2) * b;  // outputs of this level: pairs x b^2
+        const int pair = tid / (b * b), rem = tid % (b * b), r = rem / b, c = rem % b;
+        const int i0 = 2 * b * pair;
+        if (tid < n) {
+            df acc = {0.f, 0.f};
+            for (int q = c; q < b; ++q)
+                df_fma_acc(acc, {lh[i0 + b + r][i0 + q], ll[i0 + b + r][i0 + q]},
+                           {ih[i0 + q][i0 + c], il[i0 + q][i0 + c]});
+            th[tid] = acc.hi;
+            tl[tid] = acc.lo;
         }
-        if (c < i && q == 0) {
-            const df v = df_neg(dfmul(part, {rh[i], rl[i]}));
-            ih[i][c] = v.hi;
-            il[i][c] = v.lo;
+        __syncthreads();
+        if (tid < n) {
+            df acc = {0.f, 0.f};
+            for (int q = 0; q <= r; ++q)
+                df_fma_acc(acc, {ih[i0 + b + r][i0 + b + q], il[i0 + b + r][i0 + b + q]},
+                           {th[pair * b * b + q * b + c], tl[pair * b * b + q * b + c]});
+            ih[i0 + b + r][i0 + c] = -acc.hi;
+            il[i0 + b + r][i0 + c] = -acc.lo;
         }
         __syncthreads();
     }
     if (blockIdx.x == 0) {
-        for (int e = tid; e < DNB * DNB; e += 256) {
+        float* __restrict__ Ih = z < mats.ninv ? pick(mats.Ih, z) : nullptr;
+        float* __restrict__ Il = z < mats.ninv ? pick(mats.Il, z) : nullptr;
+        for (int e = tid; e < DNB * DNB; e += PANEL_THREADS) {
             const int i = e / DNB, j = e % DNB;
             if (i < nb && j < nb) {
                 const int64_t off = (k0 + i) * S + k0 + j;
                 Lh[off] = j <= i ? lh[i][j] : 0.f;
                 Ll[off] = j <= i ? ll[i][j] : 0.f;
+                if (Ih) {
+                    Ih[off] = ih[i][j];
+                    Il[off] = il[i][j];
+                }
             }
             dh[e] = ih[i][j];
             dl[e] = il[i][j];
         }
         return;
     }
-    const int i = tid >> 2, qq = tid & 3;  // 64 rows x 4 column groups of 8
-    df out[8];
+    // out[row][c] = sum_{p <= c} x[row][p] X[c][p]: warp w takes columns w and
+    // 31 - w, lane l rows l and l + 32
+    const int w = tid >> 5, lane = tid & 31;
 #pragma unroll
-    for (int t = 0; t < 8; ++t) out[t] = {0.f, 0.f};
-    for (int p = 0; p < DNB; ++p) {
-        const df x = {xh[i][p], xl[i][p]};
-#pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            const int cc = qq + 4 * t;
-            if (p <= cc) df_fma_acc(out[t], x, {ih[cc][p], il[cc][p]});
+    for (int h = 0; h < 2; ++h) {
+        const int c = h == 0 ? w : DNB - 1 - w;
+        df o0 = {0.f, 0.f}, o1 = {0.f, 0.f};
+        for (int p0 = 0; p0 <= c; p0 += 8) {
+            const int p1 = p0 + 8 <= c + 1 ? p0 + 8 : c + 1;
+            for (int p = p0; p < p1; ++p) {
+                const df y = {ih[c][p], il[c][p]};
+                df_fma_lazy(o0, {xh[lane][p], xl[lane][p]}, y);
+                df_fma_lazy(o1, {xh[lane + 32][p], xl[lane + 32][p]}, y);
+            }
+            df_renorm(o0);
+            df_renorm(o1);
         }
-    }
-    const int64_t r = r0 + i;
-    if (r < S)
-#pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            const int cc = qq + 4 * t;
-            if (cc < nb) {
-                Lh[r * S + k0 + cc] = out[t].hi;
-                Ll[r * S + k0 + cc] = out[t].lo;
+        if (c < nb) {
+            const int64_t ra = r0 + lane, rb = r0 + lane + 32;
+            if (ra < S) {
+                Lh[ra * S + k0 + c] = o0.hi;
+                Ll[ra * S + k0 + c] = o0.lo;
+            }
+            if (rb < S) {
+                Lh[rb * S + k0 + c] = o1.hi;
+                Ll[rb * S + k0 + c] = o1.lo;
             }
         }
+    }
 }
 
 // Trailing update of one Cholesky step: C (lower 32 x 32 tiles of the r x r
 // trailing matrix) -= P P^T with P the r x 32 solved panel.  128 threads, 8
 // outputs each; small register and shared footprint so several blocks share
-// an SM and the late, small steps still fill the GPU.
+// an SM and the late, small steps still fill the GPU.  `part` selects the
+// tiles: all of them (UPD_ALL), the first tile column only (UPD_NEXT: the next
+// panel, on the critical path) or every other column (UPD_REST).
+enum UpdatePart { UPD_ALL = 0, UPD_NEXT = 1, UPD_REST = 2 };
+
 __global__ void __launch_bounds__(128)
-    dfsyrk_update_kernel(DfMats mats, int64_t S, int64_t k0) {
-    float* __restrict__ Lh = mats.Lh[blockIdx.y];
-    float* __restrict__ Ll = mats.Ll[blockIdx.y];
+    dfsyrk_update_kernel(DfMats mats, int64_t S, int64_t k0, int part) {
+    float* __restrict__ Lh = pick(mats.Lh, blockIdx.y);
+    float* __restrict__ Ll = pick(mats.Ll, blockIdx.y);
     __shared__ float pih[32][33], pil[32][33], pjh[32][33], pjl[32][33];
     const int64_t r0 = k0 + DNB;
     int64_t ti, tj;
-    lower_tile_df(blockIdx.x, ti, tj);
+    if (part == UPD_NEXT) {
+        ti = blockIdx.x;
+        tj = 0;
+    } else {
+        lower_tile_df(blockIdx.x, ti, tj);
+        if (part == UPD_REST) {
+            ++ti;
+            ++tj;
+        }
+    }
     const int64_t i0 = r0 + ti * 32, j0 = r0 + tj * 32;
     const int tid = threadIdx.x;
+    const int ty = tid >> 3, tx = tid & 7;  // rows ty, ty+16; columns tx, tx+8, tx+16, tx+24
+    // the outputs' current values are fetched first so their latency overlaps the tile loads
+    df cur[2][4];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int64_t gi = i0 + ty + 16 * a, gj = j0 + tx + 8 * b;
+            const bool in = gi < S && gj < S && gj <= gi;
+            cur[a][b] = in ? df{Lh[gi * S + gj], Ll[gi * S + gj]} : df{0.f, 0.f};
+        }
     for (int e = tid; e < 32 * 32; e += 128) {
         const int a = e >> 5, b = e & 31;
         const bool ii = i0 + a < S, jj = j0 + a < S;
@@ -453,7 +515,6 @@ __global__ void __launch_bounds__(128)
         pjl[a][b] = jj ? Ll[(j0 + a) * S + k0 + b] : 0.f;
     }
     __syncthreads();
-    const int ty = tid >> 3, tx = tid & 7;  // rows ty, ty+16; columns tx, tx+8, tx+16, tx+24
     df acc[2][4];
 #pragma unroll
     for (int a = 0; a < 2; ++a)
@@ -482,7 +543,7 @@ __global__ void __launch_bounds__(128)
         for (int b = 0; b < 4; ++b) {
             const int64_t gi = i0 + ty + 16 * a, gj = j0 + tx + 8 * b;
             if (gi < S && gj < S && gj <= gi) {
-                const df v = df_add({Lh[gi * S + gj], Ll[gi * S + gj]}, df_neg(acc[a][b]));
+                const df v = df_add(cur[a][b], df_neg(acc[a][b]));
                 Lh[gi * S + gj] = v.hi;
                 Ll[gi * S + gj] = v.lo;
             }
@@ -509,30 +570,15 @@ __global__ void df_logdet_kernel(const double* __restrict__ piv, int64_t S, doub
 
 // ---------------------------------------------------- triangular inverse
 
-__global__ void df_linv_init_kernel(DfMats mats, int64_t S) {
-    float* __restrict__ Ih = mats.Ih[blockIdx.y];
-    float* __restrict__ Il = mats.Il[blockIdx.y];
-    const float* __restrict__ dh = mats.dh[blockIdx.y];
-    const float* __restrict__ dl = mats.dl[blockIdx.y];
-    const int64_t kb = blockIdx.x, k0 = kb * DNB;
-    for (int e = threadIdx.x; e < DNB * DNB; e += blockDim.x) {
-        const int i = e / DNB, j = e % DNB;
-        if (k0 + i < S && k0 + j < S) {
-            Ih[(k0 + i) * S + k0 + j] = dh[kb * DNB * DNB + e];
-            Il[(k0 + i) * S + k0 + j] = dl[kb * DNB * DNB + e];
-        }
-    }
-}
-
 // see trtri_step_kernel (linalg.cu): accumulate L[ti][kb] X[kb][tj]; block row kb + 1 applies -dinv
 __global__ void __launch_bounds__(256)
     df_trtri_step_kernel(DfMats mats, int64_t S, int64_t kb) {
-    const float* __restrict__ Lh = mats.Lh[blockIdx.y];
-    const float* __restrict__ Ll = mats.Ll[blockIdx.y];
-    float* __restrict__ Ih = mats.Ih[blockIdx.y];
-    float* __restrict__ Il = mats.Il[blockIdx.y];
-    const float* __restrict__ dh = mats.dh[blockIdx.y];
-    const float* __restrict__ dl = mats.dl[blockIdx.y];
+    const float* __restrict__ Lh = pick(mats.Lh, blockIdx.y);
+    const float* __restrict__ Ll = pick(mats.Ll, blockIdx.y);
+    float* __restrict__ Ih = pick(mats.Ih, blockIdx.y);
+    float* __restrict__ Il = pick(mats.Il, blockIdx.y);
+    const float* __restrict__ dh = pick(mats.dh, blockIdx.y);
+    const float* __restrict__ dl = pick(mats.dl, blockIdx.y);
     __shared__ float ah[32][33], al[32][33], bh[32][33], bl[32][33];
     const int64_t nbt = (S + DNB - 1) / DNB;
     const int64_t ncol = kb + 1;
@@ -555,9 +601,18 @@ __global__ void __launch_bounds__(256)
     for (int t = 0; t < 4; ++t) {
         const int c = q + 8 * t;
         const bool in = i0 + r < S && j0 + c < S;
-        df s = in ? df{Ih[(i0 + r) * S + j0 + c], Il[(i0 + r) * S + j0 + c]} : df{0.f, 0.f};
-        for (int p = 0; p < DNB; ++p) df_fma_acc(s, {ah[r][p], al[r][p]}, {bh[p][c], bl[p][c]});
-        acc[t] = s;
+        acc[t] = in ? df{Ih[(i0 + r) * S + j0 + c], Il[(i0 + r) * S + j0 + c]} : df{0.f, 0.f};
+    }
+#pragma unroll
+    for (int p0 = 0; p0 < DNB; p0 += 8) {
+#pragma unroll
+        for (int p = p0; p < p0 + 8; ++p) {
+            const df x = {ah[r][p], al[r][p]};
+#pragma unroll
+            for (int t = 0; t < 4; ++t) df_fma_lazy(acc[t], x, {bh[p][q + 8 * t], bl[p][q + 8 * t]});
+        }
+#pragma unroll
+        for (int t = 0; t < 4; ++t) df_renorm(acc[t]);
     }
     if (ti != kb + 1) {
 #pragma unroll
@@ -723,72 +778,86 @@ static DfMats mats_of(DfSpd* const* w, int count) {
     return m;
 }
 
-// L (in w[z]) = chol(A[z]) for z < count (1 or 2); A given as planes (copied unless it is w's own L)
-int dfspd_factor_n(const float* const* Ah, const float* const* Al, int count, int64_t S, DfSpd* const* w,
-                   double* const* logdet, int* info, cudaStream_t st) {
+// L (in w[z]) = chol(A[z]) for z < count (1 or 2), and L^-1 for z < n_inverse; A given as planes
+// (copied unless it is w's own L).
+//
+// Three lanes forked from st (lanes.cu).  Lane 0 carries the critical chain:
+// the pivot panel of step k, then the update of block column k + 1 alone, so
+// panel k + 1 can start at once.  Lane 1 applies the rest of step k's trailing
+// update meanwhile; lane 0 waits for it before touching column k + 2.  Lane 2
+// runs the block forward substitution for L^-1: its step k needs block column
+// k of L and the diagonal inverse of block k + 1, both final once panel k + 1
+// is done, so it trails the factorisation by one panel.
+int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int count, int n_inverse, int64_t S,
+                          DfSpd* const* w, double* const* logdet, int* info, cudaStream_t st) {
     if (S <= 0) return AJ_OK;
-    if (count < 1 || count > 2) return AJ_ERR_ARG;
+    if (count < 1 || count > 2 || n_inverse < 0 || n_inverse > count) return AJ_ERR_ARG;
+    dim3 zg(blocks_for(S, 256, 8), (unsigned)(S < 65535 ? S : 65535));
     for (int z = 0; z < count; ++z) {
         if (Ah[z] != w[z]->Lh) {
             if (cudaMemcpyAsync(w[z]->Lh, Ah[z], sizeof(float) * S * S, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
                 cudaMemcpyAsync(w[z]->Ll, Al[z], sizeof(float) * S * S, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
                 return AJ_ERR_CUDA;
         }
+        // the factorisation reads and writes only the lower triangle
+        df_zero_upper_kernel<<<zg, 256, 0, st>>>(w[z]->Lh, w[z]->Ll, S);
+        AJ_LAUNCHED();
     }
-    const DfMats m = mats_of(w, count);
+    for (int z = 0; z < n_inverse; ++z) {
+        if (!w[z]->Ih) return AJ_ERR_ARG;
+        if (cudaMemsetAsync(w[z]->Ih, 0, sizeof(float) * 2 * S * S, st) != cudaSuccess) return AJ_ERR_CUDA;
+    }
+    DfMats m = mats_of(w, count);
+    m.ninv = n_inverse;
+    Lanes* lanes = nullptr;
+    AJ_TRY(lanes_for(st, &lanes));
+    Lanes& ln = *lanes;
+    const int nlanes = n_inverse > 0 ? 3 : 2;
+    AJ_TRY(lanes_fork(ln, st, nlanes));
+    cudaStream_t crit = ln.s[0], bulk = ln.s[1], tri = ln.s[2];
     const int64_t nbt = (S + DNB - 1) / DNB;
-    for (int64_t kb = 0; kb < nbt; ++kb) {
+    auto panel = [&](int64_t kb) {
         const int64_t k0 = kb * DNB;
         const int64_t below = S - k0 - DNB;
         const unsigned g = 1 + (unsigned)(below > 0 ? (below + 63) / 64 : 0);
-        dfchol_panel_kernel<<<dim3(g, count), 256, 0, st>>>(m, S, k0, info);
+        dfchol_panel_kernel<<<dim3(g, count), PANEL_THREADS, 0, crit>>>(m, S, k0, info);
+        return check_launch();
+    };
+    AJ_TRY(panel(0));
+    for (int64_t kb = 0; kb + 1 < nbt; ++kb) {
+        const int64_t k0 = kb * DNB;
+        const int64_t tb = (S - k0 - DNB + 31) / 32;  // trailing tile rows (>= 1 here)
+        dfsyrk_update_kernel<<<dim3((unsigned)tb, count), 128, 0, crit>>>(m, S, k0, UPD_NEXT);
         AJ_LAUNCHED();
-        if (below > 0) {
-            const int64_t tb = (below + 31) / 32;
-            dfsyrk_update_kernel<<<dim3((unsigned)(tb * (tb + 1) / 2), count), 128, 0, st>>>(m, S, k0);
+        if (tb > 1) {
+            AJ_TRY(lane_signal(ln, kEvPanel, 0));
+            AJ_TRY(lane_wait(ln, 1, kEvPanel));
+            dfsyrk_update_kernel<<<dim3((unsigned)((tb - 1) * tb / 2), count), 128, 0, bulk>>>(m, S, k0, UPD_REST);
+            AJ_LAUNCHED();
+            AJ_TRY(lane_signal(ln, kEvUpdate, 1));
+        }
+        AJ_TRY(panel(kb + 1));
+        if (n_inverse > 0) {
+            AJ_TRY(lane_signal(ln, kEvDiag, 0));
+            AJ_TRY(lane_wait(ln, 2, kEvDiag));
+            const int64_t tiles = (nbt - kb - 1) * (kb + 1);
+            df_trtri_step_kernel<<<dim3((unsigned)tiles, n_inverse), 256, 0, tri>>>(m, S, kb);
             AJ_LAUNCHED();
         }
+        if (tb > 1) AJ_TRY(lane_wait(ln, 0, kEvUpdate));
     }
-    dim3 zg(blocks_for(S, 256, 8), (unsigned)(S < 65535 ? S : 65535));
-    for (int z = 0; z < count; ++z) {
-        df_zero_upper_kernel<<<zg, 256, 0, st>>>(w[z]->Lh, w[z]->Ll, S);
-        AJ_LAUNCHED();
+    for (int z = 0; z < count; ++z)
         if (logdet && logdet[z]) {
-            df_logdet_kernel<<<1, 1024, 0, st>>>(w[z]->piv, S, logdet[z], info);
+            df_logdet_kernel<<<1, 1024, 0, crit>>>(w[z]->piv, S, logdet[z], info);
             AJ_LAUNCHED();
         }
-    }
-    return AJ_OK;
+    return lanes_join(ln, st, nlanes);
 }
 
 int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* logdet, int* info, cudaStream_t st) {
     DfSpd* ws[1] = {&w};
     double* ld[1] = {logdet};
-    return dfspd_factor_n(&Ah, &Al, 1, S, ws, ld, info, st);
-}
-
-int dfspd_invert_factor_n(int64_t S, DfSpd* const* w, int count, cudaStream_t st) {
-    if (S <= 0) return AJ_OK;
-    if (count < 1 || count > 2) return AJ_ERR_ARG;
-    for (int z = 0; z < count; ++z) {
-        if (!w[z]->Ih) return AJ_ERR_ARG;
-        if (cudaMemsetAsync(w[z]->Ih, 0, sizeof(float) * 2 * S * S, st) != cudaSuccess) return AJ_ERR_CUDA;
-    }
-    const DfMats m = mats_of(w, count);
-    const int64_t nbt = (S + DNB - 1) / DNB;
-    df_linv_init_kernel<<<dim3((unsigned)nbt, count), 256, 0, st>>>(m, S);
-    AJ_LAUNCHED();
-    for (int64_t kb = 0; kb + 1 < nbt; ++kb) {
-        const int64_t tiles = (nbt - kb - 1) * (kb + 1);
-        df_trtri_step_kernel<<<dim3((unsigned)tiles, count), 256, 0, st>>>(m, S, kb);
-        AJ_LAUNCHED();
-    }
-    return AJ_OK;
-}
-
-int dfspd_invert_factor(int64_t S, DfSpd& w, cudaStream_t st) {
-    DfSpd* ws[1] = {&w};
-    return dfspd_invert_factor_n(S, ws, 1, st);
+    return dfspd_factor_invert_n(&Ah, &Al, 1, 0, S, ws, ld, info, st);
 }
 
 int dfspd_inverse_from_factor(int64_t S, DfSpd& w, float* Ah, float* Al, cudaStream_t st) {
@@ -853,8 +922,11 @@ int aj_spd_inverse_mixed(const double* A, int64_t S, double* Ainv, double* logde
     Carver sc(sub, dfspd_bytes(S, true));
     DfSpd w = dfspd_carve(sc, S, true);
     AJ_TRY(df_split(A, S * S, Ap, Ap + S * S, st));
-    AJ_TRY(dfspd_factor(Ap, Ap + S * S, S, w, logdet, info, st));
-    AJ_TRY(dfspd_invert_factor(S, w, st));
+    const float* ah[1] = {Ap};
+    const float* al[1] = {Ap + S * S};
+    DfSpd* ws[1] = {&w};
+    double* ld[1] = {logdet};
+    AJ_TRY(dfspd_factor_invert_n(ah, al, 1, 1, S, ws, ld, info, st));
     AJ_TRY(dfspd_inverse_from_factor(S, w, Ip, Ip + S * S, st));
     return df_join(Ip, Ip + S * S, S * S, Ainv, st);
 }

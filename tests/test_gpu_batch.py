@@ -1,0 +1,127 @@
+"""Batched evaluations: many lens models (own S, mapping, neighbours, coefficient) against one dataset.
+
+Each model's logE, dlogE/dlambda and weight gradient from one
+aj_log_evidence_batched call (eagerly and replayed from a captured graph) is
+checked against the float64 oracle at the single-evaluation tolerances:
+rel 1e-10 for the float64 path, the mixed-path bounds of test_gpu_mixed.py
+for the mixed one.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import adjoint
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def setup():
+    import autojax_gb300 as aj
+    from autojax_gb300 import synthetic
+
+    d = synthetic.make_dataset("cfg1", K=600, seed=5)
+    W = aj.w_tilde_curvature_interferometer_from(d["noise_map_real"], d["uv_wavelengths"], d["grid_radians_slim"])
+    models = synthetic.lens_models(d, 7, S_range=(20, 180), lam_range=(1e-2, 1e2), seed=9)
+    refs = [adjoint.log_evidence_and_grad(d["dirty_image"], d["data"], d["noise_map"], W,
+                                          m["pix_indexes_for_sub_slim_index"], m["pix_weights_for_sub_slim_index"],
+                                          m["neighbors"], m["neighbors_sizes"], coefficient=m["coefficient"])
+            for m in models]
+    return d, W, models, refs
+
+
+def _batch(setup, precision):
+    from autojax_gb300.inversion import Dataset, LogEvidenceBatch
+
+    d, W, models, _ = setup
+    ds = Dataset(d["dirty_image"], d["data"], d["noise_map"], W, precision=precision)
+    P = max(m["neighbors"].shape[1] for m in models)
+    batch = LogEvidenceBatch(ds, [m["S"] for m in models], B=3, P=P)
+    for i, m in enumerate(models):
+        batch.set_model(i, m["pix_indexes_for_sub_slim_index"], m["pix_weights_for_sub_slim_index"], m["neighbors"],
+                        m["neighbors_sizes"], m["coefficient"])
+    return batch
+
+
+def _cond(setup, m):
+    from oracle import numpy_port as ref
+
+    W = setup[1]
+    T = ref.mapping_matrix_from(m["pix_indexes_for_sub_slim_index"], m["pix_weights_for_sub_slim_index"], m["S"])
+    H = ref.constant_regularization_matrix_from(m["coefficient"], m["neighbors"], m["neighbors_sizes"])
+    ev = np.linalg.eigvalsh(T.T @ W @ T + H)
+    return ev[-1] / ev[0]
+
+
+def _check(batch, setup, precision):
+    import torch
+
+    _, _, models, refs = setup
+    torch.cuda.synchronize()
+    batch.check()
+    out = batch.out.cpu().numpy()
+    for i, (m, (r_logE, r_dlam, r_gw)) in enumerate(zip(models, refs)):
+        gw = batch.evals[i].grad_weights.cpu().numpy()
+        if precision == "fp64":
+            assert abs(out[i, 0] - r_logE) <= 1e-10 * abs(r_logE), (i, out[i, 0], r_logE)
+            assert abs(out[i, 1] - r_dlam) <= 1e-8 * max(1.0, abs(r_dlam)), (i, out[i, 1], r_dlam)
+            np.testing.assert_allclose(gw, r_gw, rtol=1e-8, atol=1e-9 * np.abs(r_gw).max())
+        else:
+            c = m["coefficient"]
+            assert abs(out[i, 0] - r_logE) <= 1e-8 * abs(r_logE), (i, out[i, 0], r_logE)
+            assert abs(out[i, 1] - r_dlam) <= 1e-6 * m["S"] / c**2 + 1e-5 * abs(r_dlam), (i, out[i, 1], r_dlam)
+            # the weight gradient goes through A^-1: its error scales with cond(A)
+            np.testing.assert_allclose(gw, r_gw, rtol=0, atol=max(1e-5, 2e-15 * _cond(setup, m)) * np.abs(r_gw).max())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_matches_oracle(setup, precision):
+    batch = _batch(setup, precision)
+    batch.launch()
+    _check(batch, setup, precision)
+
+
+def test_batch_graph_replay_matches_oracle(setup):
+    import torch
+
+    batch = _batch(setup, "mixed")
+    batch.capture()
+    batch.out.zero_()
+    for e in batch.evals:
+        e.grad_weights.zero_()
+    batch.step()
+    _check(batch, setup, "mixed")
+    assert batch.launches_per_batch and batch.launches_per_batch > 10 * batch.n
+    # new coefficients go through the captured graph
+    _, _, models, _ = setup
+    for i, m in enumerate(models):
+        batch.evals[i].set_coefficient(m["coefficient"] * 1.5)
+    batch.step()
+    torch.cuda.synchronize()
+    d, W = setup[0], setup[1]
+    for i in (0, len(models) - 1):
+        m = models[i]
+        r = adjoint.log_evidence_and_grad(d["dirty_image"], d["data"], d["noise_map"], W,
+                                          m["pix_indexes_for_sub_slim_index"], m["pix_weights_for_sub_slim_index"],
+                                          m["neighbors"], m["neighbors_sizes"], coefficient=m["coefficient"] * 1.5)
+        assert abs(float(batch.out[i, 0]) - r[0]) <= 1e-8 * abs(r[0])
+
+
+def test_batch_rejects_a_short_workspace(setup):
+    import ctypes
+
+    import torch
+
+    from autojax_gb300 import _lib
+
+    batch = _batch(setup, "fp64")
+    batch._ws_bytes[2] = 16
+    rc = batch.lib.aj_log_evidence_batched(batch._problems, batch.n, _lib.AJ_FP64, 1, batch.out.data_ptr(),
+                                           ctypes.cast(batch._grads, ctypes.c_void_p),
+                                           ctypes.cast(batch._recons, ctypes.c_void_p),
+                                           ctypes.cast(batch._ws, ctypes.c_void_p),
+                                           ctypes.cast(batch._ws_bytes, ctypes.c_void_p), batch.info.data_ptr(),
+                                           torch.cuda.current_stream().cuda_stream)
+    assert rc == _lib.AJ_ERR_WORKSPACE

@@ -111,3 +111,66 @@ def test_mixed_w_tilde_matches_oracle(aj, M, K):
     scale = np.abs(exp).max()
     np.testing.assert_allclose(W, exp, rtol=0, atol=1e-12 * scale)
     np.testing.assert_allclose(P[0].astype(np.float64) + P[1].astype(np.float64), W, rtol=0, atol=1e-15 * scale)
+
+
+def _spd_with_condition(S, cond, seed):
+    rng = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rng.standard_normal((S, S)))
+    ev = np.logspace(0.0, np.log10(cond), S)
+    return (Q * ev) @ Q.T
+
+
+@pytest.mark.parametrize("S", [1, 31, 32, 33, 100, 257, 1000])
+def test_mixed_spd_inverse_matches_numpy(S):
+    """aj_spd_inverse_mixed (double-float Cholesky, L^-1 and L^-T L^-1) against float64 LAPACK.
+
+    Tolerance: each double-float operation keeps ~2^-47, so the inverse is good
+    to ~S 2^-47 cond(A) of its largest entry; log det to ~S 2^-47 cond(A).
+    """
+    import torch
+
+    from autojax_gb300 import _lib
+
+    lib = _lib.load()
+    cond = 1e6
+    A = _spd_with_condition(S, cond, 7 + S)
+    At = torch.from_numpy(A).cuda()
+    inv = torch.empty_like(At)
+    logdet = torch.zeros(1, dtype=torch.float64, device="cuda")
+    info = torch.zeros(2, dtype=torch.int32, device="cuda")
+    ws = torch.empty(lib.aj_spd_inverse_mixed_workspace_size(S), dtype=torch.uint8, device="cuda")
+    _lib.check(lib.aj_spd_inverse_mixed(At.data_ptr(), S, inv.data_ptr(), logdet.data_ptr(), ws.data_ptr(),
+                                        ws.numel(), info.data_ptr(), torch.cuda.current_stream().cuda_stream),
+               "aj_spd_inverse_mixed")
+    torch.cuda.synchronize()
+    assert int(info[0]) == 0
+    ref = np.linalg.inv(A)
+    got = inv.cpu().numpy()
+    tol = max(S, 32) * 2.0**-47 * cond * np.abs(ref).max()
+    assert np.abs(got - ref).max() <= tol
+    assert np.abs(got - got.T).max() == 0.0
+    sign, ld = np.linalg.slogdet(A)
+    assert sign > 0
+    assert abs(float(logdet[0]) - ld) <= max(S, 32) * 2.0**-47 * cond * max(1.0, abs(ld))
+
+
+def test_mixed_spd_inverse_reports_not_positive_definite():
+    import torch
+
+    from autojax_gb300 import _lib
+
+    lib = _lib.load()
+    S = 70
+    A = _spd_with_condition(S, 10.0, 3)
+    A[40, 40] = -1.0  # leading minor 41 is indefinite
+    At = torch.from_numpy(A).cuda()
+    inv = torch.empty_like(At)
+    logdet = torch.zeros(1, dtype=torch.float64, device="cuda")
+    info = torch.zeros(2, dtype=torch.int32, device="cuda")
+    ws = torch.empty(lib.aj_spd_inverse_mixed_workspace_size(S), dtype=torch.uint8, device="cuda")
+    _lib.check(lib.aj_spd_inverse_mixed(At.data_ptr(), S, inv.data_ptr(), logdet.data_ptr(), ws.data_ptr(),
+                                        ws.numel(), info.data_ptr(), torch.cuda.current_stream().cuda_stream),
+               "aj_spd_inverse_mixed")
+    torch.cuda.synchronize()
+    assert int(info[0]) == _lib.AJ_INFO_NOT_POSITIVE_DEFINITE
+    assert np.isnan(float(logdet[0]))
