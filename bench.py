@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--stages", action="store_true", help="also time the pipeline stages separately")
     ap.add_argument("--skip-batch", action="store_true", help="omit the batched many-model measurement")
     ap.add_argument("--batch", type=int, default=64, help="lens models in the batched measurement")
+    ap.add_argument("--only", choices=("roofline", "wtilde"), help="run one kernel measurement alone (for ncu)")
     return ap.parse_args()
 
 
@@ -229,6 +230,93 @@ def time_region(fn, steps: int, dist: Dist, name: str = "region") -> float:
     return dist.max(e0.elapsed_time(e1) / 1e3)
 
 
+# DRAM bytes (read + write) of one aj_spd_inverse_mixed call at S = 1,500, summed
+# over its launches, from the ncu capture in
+# profiles/spd_inverse_mixed_s1500_traffic.md (the group is L2-resident: its
+# working set, 7 float planes of S x S, is 63 MB).
+ROOFLINE_TRAFFIC_BYTES = None
+
+
+def roofline(A, dist: Dist):
+    """Roofline of the dominant kernel group of the mixed path: the double-float
+    factorisation chain (Cholesky panel, trailing updates, triangular inverse,
+    L^-T L^-1), run standalone through aj_spd_inverse_mixed on the S x S matrix
+    A and timed with CUDA events on the launching stream.
+
+    Algorithmic work: S^3 float64-class flops (S^3/3 each for the factor, the
+    inverse factor and L^-T L^-1).  Peak: the measured float32 FMA rate over the
+    11.4 float32 instructions one double-float multiply-add takes (2 flops).
+    The float64 path's aj_spd_inverse does the same work on the FP64 pipe.
+    """
+    import torch
+
+    from autojax_gb300 import _lib
+
+    lib = _lib.load()
+    dev = A.device
+    S = A.shape[0]
+    Ainv = torch.empty((S, S), dtype=torch.float64, device=dev)
+    ld = torch.empty(1, dtype=torch.float64, device=dev)
+    info = torch.zeros(2, dtype=torch.int32, device=dev)
+    stc = torch.cuda.current_stream().cuda_stream
+    ws_m = torch.empty(lib.aj_spd_inverse_mixed_workspace_size(S), dtype=torch.uint8, device=dev)
+    ws_f = torch.empty(lib.aj_spd_inverse_workspace_size(S), dtype=torch.uint8, device=dev)
+
+    def inv_mixed(i):
+        _lib.check(lib.aj_spd_inverse_mixed(A.data_ptr(), S, Ainv.data_ptr(), ld.data_ptr(), ws_m.data_ptr(),
+                                            ws_m.numel(), info.data_ptr(), stc), "aj_spd_inverse_mixed")
+
+    def inv_fp64(i):
+        _lib.check(lib.aj_spd_inverse(A.data_ptr(), S, Ainv.data_ptr(), ld.data_ptr(), ws_f.data_ptr(), ws_f.numel(),
+                                      info.data_ptr(), stc), "aj_spd_inverse")
+
+    for i in range(3):
+        inv_mixed(i)
+        inv_fp64(i)
+    torch.cuda.synchronize()
+    if int(info[0]) != 0:
+        raise RuntimeError(f"roofline matrix not positive definite (info {info.tolist()})")
+    reps = 5
+    t_inv_mixed = time_region(inv_mixed, reps, dist, "roofline_mixed") / reps
+    t_inv_fp64 = time_region(inv_fp64, reps, dist, "roofline_fp64") / reps
+    fp64_peak = fma_peak_tflops(_lib.AJ_FP64)
+    fp32_peak = fma_peak_tflops(_lib.AJ_MIXED)
+    df_peak = fp32_peak / 11.4
+    inv_flops = float(S) ** 3
+    achieved = inv_flops / t_inv_mixed / 1e12
+    roof = {
+        "kernel": "double-float Cholesky + triangular inverse + L^-T L^-1 of A (aj_spd_inverse_mixed: "
+                  "dfchol_panel, dfsyrk_update, df_trtri_step, df_lauum_row)",
+        "bound": "fp32 (double-float)",
+        "achieved": achieved,
+        "peak": df_peak,
+        "unit": "TFLOP/s (float64-class)",
+        "frac": achieved / df_peak,
+        "peak_source": "measured in this run: aj_probe_fma float32 FMA rate / 11.4 float32 instructions "
+                       "per double-float multiply-add",
+        "traffic": ROOFLINE_TRAFFIC_BYTES,
+        "S": S,
+        "ms": 1e3 * t_inv_mixed,
+        "fp64_same_work_ms": 1e3 * t_inv_fp64,
+        "fp64_same_work_frac_of_fp64_peak": inv_flops / t_inv_fp64 / 1e12 / fp64_peak,
+    }
+    return roof, fp64_peak, fp32_peak
+
+
+def roofline_only(args, dist: Dist) -> dict:
+    """The roofline group alone on a synthetic SPD matrix of the workload's S (the
+    kernels' work does not depend on the values): a small-memory run for ncu."""
+    import torch
+
+    torch.cuda.set_device(dist.local)
+    S = 1500
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal((S, S))
+    A = torch.from_numpy(X @ X.T / S + np.eye(S)).cuda()
+    roof, fp64_peak, fp32_peak = roofline(A, dist)
+    return {"roofline": roof, "peaks": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak}}
+
+
 def gpu_arm(args, dist: Dist) -> dict:
     import torch
 
@@ -300,43 +388,14 @@ def gpu_arm(args, dist: Dist) -> dict:
         e.evaluate_host(*mods[i % len(mods)])
     t_e2e = dist.max(time.perf_counter() - t0)
 
-    # Roofline of the dominant kernel group of the headline (mixed) path: the double-float
-    # factorisation kernels (Cholesky panel + trailing update + triangular inverse, plus
-    # L^-T L^-1), timed standalone on this workload's A with CUDA events.  Algorithmic work
-    # S^3 (S^3/3 each for the factor, the inverse factor and L^-T L^-1) in float64-class
-    # flops; the double-float peak is the measured float32 FMA rate over the 11.4 float32
-    # instructions one double-float multiply-add takes (2 flops).
+    # roofline of the dominant kernel group, timed standalone on this workload's A = F + H
     A = torch.from_numpy(aj.constant_regularization_matrix_from(1.0, d["neighbors"], d["neighbors_sizes"])).to(dev)
     F = aj.curvature_matrix_via_w_wilde_sparse_mapping_matrix_from(
         w_tilde, torch.from_numpy(d["pix_indexes_for_sub_slim_index"]).to(dev),
         torch.from_numpy(d["pix_weights_for_sub_slim_index"]).to(dev), S)
     A = (A + F).contiguous()
-    Ainv = torch.empty((S, S), dtype=torch.float64, device=dev)
-    ld = torch.empty(1, dtype=torch.float64, device=dev)
-    info = torch.zeros(2, dtype=torch.int32, device=dev)
-    stc = torch.cuda.current_stream().cuda_stream
-    ws_m = torch.empty(lib.aj_spd_inverse_mixed_workspace_size(S), dtype=torch.uint8, device=dev)
-    ws_f = torch.empty(lib.aj_spd_inverse_workspace_size(S), dtype=torch.uint8, device=dev)
-
-    def inv_mixed(i):
-        _lib.check(lib.aj_spd_inverse_mixed(A.data_ptr(), S, Ainv.data_ptr(), ld.data_ptr(), ws_m.data_ptr(),
-                                            ws_m.numel(), info.data_ptr(), stc), "aj_spd_inverse_mixed")
-
-    def inv_fp64(i):
-        _lib.check(lib.aj_spd_inverse(A.data_ptr(), S, Ainv.data_ptr(), ld.data_ptr(), ws_f.data_ptr(), ws_f.numel(),
-                                      info.data_ptr(), stc), "aj_spd_inverse")
-
-    for i in range(2):
-        inv_mixed(i)
-        inv_fp64(i)
-    reps = 5
-    t_inv_mixed = time_region(inv_mixed, reps, dist, "roofline_mixed") / reps
-    t_inv_fp64 = time_region(inv_fp64, reps, dist, "roofline_fp64") / reps
-    fp64_peak = fma_peak_tflops(_lib.AJ_FP64)
-    fp32_peak = fma_peak_tflops(_lib.AJ_MIXED)
-    df_peak = fp32_peak / 11.4
-    inv_flops = float(S) ** 3
-    achieved = inv_flops / t_inv_mixed / 1e12
+    roof, fp64_peak, fp32_peak = roofline(A, dist)
+    del F
 
     result = {
         "metric": METRIC,
@@ -365,21 +424,7 @@ def gpu_arm(args, dist: Dist) -> dict:
         "e2e": {"value": args.steps * dist.world / t_e2e, "unit": "evals/s", "h2d_bytes_per_step": e.h2d_bytes(),
                 "d2h_bytes_per_step": e.d2h_bytes()},
         "gpu_launches": (ev["mixed"].launches_per_eval or 0) * args.steps,
-        "roofline": {
-            "kernel": "double-float Cholesky + triangular inverse + L^-T L^-1 of A (aj_spd_inverse_mixed: "
-                      "dfchol_panel, dfsyrk_update, df_trtri_step, gemm_df)",
-            "bound": "fp32 (double-float)",
-            "achieved": achieved,
-            "peak": df_peak,
-            "unit": "TFLOP/s (float64-class)",
-            "frac": achieved / df_peak,
-            "peak_source": "measured in this run: aj_probe_fma float32 FMA rate / 11.4 float32 instructions "
-                           "per double-float multiply-add",
-            "traffic": None,
-            "ms": 1e3 * t_inv_mixed,
-            "fp64_same_work_ms": 1e3 * t_inv_fp64,
-            "fp64_same_work_frac_of_fp64_peak": inv_flops / t_inv_fp64 / 1e12 / fp64_peak,
-        },
+        "roofline": roof,
         "peaks": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak,
                   "hbm_gbs": measured_peaks().get("hbm_gbs"), "bf16_tflops": measured_peaks().get("bf16_tflops")},
         "clocks": clocks,
@@ -389,7 +434,7 @@ def gpu_arm(args, dist: Dist) -> dict:
     if args.stages:
         result["stages_ms"] = stage_times(d, w_tilde, dev, dist)
     if not args.skip_batch:
-        del ev, A, F, Ainv, ws_m, ws_f, w_tilde, w_compact
+        del ev, A, w_tilde, w_compact
         torch.cuda.empty_cache()
         result["batched"] = batched_bench(args, dev, dist)
     return result
@@ -595,8 +640,17 @@ def main():
                 return
             print(json.dumps(reference_arm(args, dist)), flush=True)
             return
-        res = gpu_arm(args, dist)
-        if dist.rank == 0 and dist.world == 1 and not args.skip_cpu:
+        if args.only == "roofline":
+            res = roofline_only(args, dist)
+        elif args.only == "wtilde":
+            import torch
+
+            torch.cuda.set_device(dist.local)
+            res = {"w_tilde": wtilde_bench(dataset(args.config), torch.device("cuda", dist.local),
+                                           fma_peak_tflops(1))}
+        else:
+            res = gpu_arm(args, dist)
+        if dist.rank == 0 and dist.world == 1 and not args.skip_cpu and not args.only:
             d = dataset(args.config)
             res["cpu_baseline"] = cpu_baseline(d, cpu_eval_setup(d))
         if dist.rank == 0:

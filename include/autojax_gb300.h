@@ -266,6 +266,39 @@ size_t aj_log_evidence_workspace_size(const aj_problem* p, int precision, int wi
 int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* out, double* grad_weights,
                     double* reconstruction, void* workspace, size_t workspace_bytes, int* info, void* stream);
 
+/* Mapping-weight builder (no reference counterpart: the reference takes
+ * pix_indexes / pix_weights as likelihood inputs, numba.py:294-376, built by
+ * PyAutoLens).  Coordinates are (y, x) pairs in one angular unit (arcsec).
+ *
+ * aj_sis_trace: beta = theta - theta_E theta / |theta|, an SIS at the origin;
+ * theta_E is read from einstein_radius_dev when that is not NULL.
+ * aj_sis_trace_vjp: dL/dtheta_E (one device double) from dL/dbeta (M, 2). */
+int aj_sis_trace(const double* theta, int64_t M, double einstein_radius, const double* einstein_radius_dev,
+                 double* beta, void* stream);
+int aj_sis_trace_vjp(const double* theta, int64_t M, const double* grad_beta, double* grad_einstein_radius,
+                     void* stream);
+
+/* Barycentric weights of the traced points in the triangulation (simplices,
+ * (T, 3) vertex indices into points (S, 2)): pix_indexes / pix_weights
+ * (M, 3).  A point maps to the first (lowest-index) triangle containing it,
+ * decided in float64 without contraction; outside the hull it maps to its
+ * nearest vertex with weight 1 and the row is -1 padded.  A simplex entry out
+ * of range sets AJ_INFO_INDEX_RANGE. */
+int aj_delaunay_weights(const double* beta, int64_t M, const double* points, int64_t S, const int64_t* simplices,
+                        int64_t T, int64_t* pix_indexes, double* pix_weights, int* info, void* stream);
+/* dL/dpoints (S, 2) and dL/dbeta (M, 2) from dL/dpix_weights (M, 3); rows
+ * outside the hull contribute nothing. */
+int aj_delaunay_weights_vjp(const double* beta, int64_t M, const double* points, int64_t S,
+                            const int64_t* pix_indexes, const double* grad_weights, double* grad_points,
+                            double* grad_beta, void* stream);
+
+/* Bilinear weights (M, 4) on the n x n rectangular mesh over [-hw, hw]^2,
+ * rows growing downwards in y, and dL/dbeta from dL/dpix_weights. */
+int aj_bilinear_weights(const double* beta, int64_t M, int64_t n, double half_width, int64_t* pix_indexes,
+                        double* pix_weights, void* stream);
+int aj_bilinear_weights_vjp(const double* beta, int64_t M, int64_t n, double half_width, const double* grad_weights,
+                            double* grad_beta, void* stream);
+
 /* Batched log-evidence: n independent lens-model evaluations in one call (no
  * reference counterpart; the reference evaluates one model per call of
  * numba.py:761-857).  problems[i] usually share dirty_image, data, noise_map

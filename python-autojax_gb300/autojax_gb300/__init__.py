@@ -58,3 +58,5 @@ NUMBA_API = (
     "log_likelihood_function_via_w_tilde_from",
     "log_likelihood_function_via_w_compact_from",
 )
+
+from . import torch_ops  # noqa: E402,F401  (registers torch.ops.autojax_gb300.*)

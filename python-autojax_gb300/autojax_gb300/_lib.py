@@ -101,6 +101,12 @@ SIGNATURES = {
     "aj_split_f64": (INT, [P, I64, P, P, P]),
     "aj_log_evidence_workspace_size": (SZ, [C.POINTER(Problem), INT, INT]),
     "aj_log_evidence": (INT, [C.POINTER(Problem), INT, INT, P, P, P, P, SZ, P, P]),
+    "aj_sis_trace": (INT, [P, I64, D, P, P, P]),
+    "aj_sis_trace_vjp": (INT, [P, I64, P, P, P]),
+    "aj_delaunay_weights": (INT, [P, I64, P, I64, P, I64, P, P, P, P]),
+    "aj_delaunay_weights_vjp": (INT, [P, I64, P, I64, P, P, P, P, P]),
+    "aj_bilinear_weights": (INT, [P, I64, I64, D, P, P, P]),
+    "aj_bilinear_weights_vjp": (INT, [P, I64, I64, D, P, P, P]),
     "aj_log_evidence_batched": (INT, [C.POINTER(Problem), I64, INT, INT, P, P, P, P, P, P, P]),
     "aj_graph_begin": (INT, [P]),
     "aj_graph_end": (INT, [P, C.POINTER(P)]),

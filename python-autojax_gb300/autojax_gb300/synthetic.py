@@ -241,14 +241,15 @@ def make_dataset(cfg: Config | str, *, K: int | None = None, S: int | None = Non
 
 
 def lens_models(d: dict, n: int, *, S_range=(500, 2000), einstein_range=(0.6, 1.2), lam_range=(1e-3, 1e3),
-                source_radius: float = 1.5, seed: int = 0) -> list[dict]:
+                seed: int = 0) -> list[dict]:
     """``n`` lens models for one dataset, as a sampler would propose them.
 
     Each model draws its source-pixel count S uniformly from ``S_range``, its
     SIS Einstein radius uniformly from ``einstein_range`` and lambda
-    log-uniformly from ``lam_range``; its S source points are uniform in a
-    disc of ``source_radius`` arcsec, and the image grid is ray-traced and
-    mapped with barycentric weights of their Delaunay triangulation.
+    log-uniformly from ``lam_range``.  Its S Delaunay vertices are traced
+    image pixels (a random subset, jittered by 1e-4"), as image-plane-derived
+    meshes place them, so every source pixel has data nearby; the image grid
+    is ray-traced and mapped with barycentric weights of their triangulation.
     """
     rng = np.random.default_rng(seed)
     theta = d["grid_radians_slim"] / ARCSEC
@@ -257,10 +258,11 @@ def lens_models(d: dict, n: int, *, S_range=(500, 2000), einstein_range=(0.6, 1.
         S = int(rng.integers(S_range[0], S_range[1] + 1))
         theta_e = float(rng.uniform(*einstein_range))
         lam = float(np.exp(rng.uniform(np.log(lam_range[0]), np.log(lam_range[1]))))
-        rr = source_radius * np.sqrt(rng.uniform(0, 1, S))
-        tt = rng.uniform(0, 2 * np.pi, S)
-        pts = np.stack([rr * np.sin(tt), rr * np.cos(tt)], axis=1)
-        pidx, pw, nb = delaunay_mesh(sis_trace(theta, theta_e), pts)
+        beta = sis_trace(theta, theta_e)
+        pick = rng.choice(beta.shape[0], size=min(S, beta.shape[0]), replace=False)
+        pts = beta[pick] + 1e-4 * rng.standard_normal((pick.size, 2))
+        S = pick.size
+        pidx, pw, nb = delaunay_mesh(beta, pts)
         out.append({
             "S": S,
             "einstein_radius": theta_e,

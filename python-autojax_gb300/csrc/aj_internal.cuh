@@ -58,8 +58,10 @@ struct DfSpd {
     float *Lh, *Ll;  // factor (S x S)
     float *Ih, *Il;  // inverse factor (S x S) or null
     float *dh, *dl;  // inverses of the diagonal blocks
+    float *fh, *fl;  // factored diagonal blocks
     double* piv;     // the S pivots L_ii in float64
     double* vec;     // S scratch
+    double* vec2;    // S scratch
 };
 size_t dfspd_bytes(int64_t S, bool with_inverse);
 DfSpd dfspd_carve(Carver& cv, int64_t S, bool with_inverse);
@@ -73,10 +75,12 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* logdet, int* info, cudaStream_t st);
 // The same for count = 1 or 2 independent matrices sharing every launch; the
 // first n_inverse of them also get their inverse factor L^-1 (in w->Ih/Il),
-// computed alongside the factorisation as its panels complete.
+// computed alongside the factorisation as its panels complete.  With AIh/AIl
+// set (planes, S x S), the first matrix's inverse A^-1 = L^-T L^-1 is built
+// up the same way, one finished block row of L^-1 at a time.
 int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int count, int n_inverse, int64_t S,
-                          DfSpd* const* w, double* const* logdet, int* info, cudaStream_t st);
-int dfspd_inverse_from_factor(int64_t S, DfSpd& w, float* Ah, float* Al, cudaStream_t st);
+                          DfSpd* const* w, double* const* logdet, int* info, cudaStream_t st, float* AIh = nullptr,
+                          float* AIl = nullptr);
 int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st);
 int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x, double* r,
                         cudaStream_t st);

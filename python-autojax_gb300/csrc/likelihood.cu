@@ -98,8 +98,15 @@ __global__ void frob_lower_kernel(const double* __restrict__ Li, int64_t S, doub
 }
 
 // out[1] = dlogE/dlambda.  L's entries follow numba.py:688-694: diag(n), -1 per neighbour entry.
+// A^-1 entry (i, j) from float64 storage, or from double-float planes when Ainv is null
+__device__ __forceinline__ double ainv_at(const double* Ainv, const float* AIh, const float* AIl, int64_t S, int64_t i,
+                                          int64_t j) {
+    return Ainv ? Ainv[i * S + j] : (double)AIh[i * S + j] + (double)AIl[i * S + j];
+}
+
 __global__ void dlam_kernel(const int64_t* __restrict__ nb, const int64_t* __restrict__ nsz, int64_t S, int64_t P,
                             const double* __restrict__ s, const double* __restrict__ Ainv,
+                            const float* __restrict__ AIh, const float* __restrict__ AIl,
                             const double* __restrict__ frob_partial, int64_t nfrob, double coef,
                             const double* __restrict__ coef_dev, const double* __restrict__ shift,
                             double* __restrict__ out) {
@@ -110,14 +117,14 @@ __global__ void dlam_kernel(const int64_t* __restrict__ nb, const int64_t* __res
     for (int64_t i = threadIdx.x; i < S; i += blockDim.x) {
         const double ni = (double)nsz[i];
         sls = fma(ni, s[i] * s[i], sls);
-        tra = fma(ni, Ainv[i * S + i], tra);
+        tra = fma(ni, ainv_at(Ainv, AIh, AIl, S, i, i), tra);
         trl += ni;
         for (int64_t j = 0; j < P; ++j) {
             const int64_t k = nb[i * P + j];
             if (k == -1) break;
             if (k < 0 || k >= S) continue;
             sls -= s[i] * s[k];
-            tra -= Ainv[k * S + i];
+            tra -= ainv_at(Ainv, AIh, AIl, S, k, i);
             if (k == i) trl -= 1.0;
         }
     }
@@ -166,6 +173,52 @@ __global__ void __launch_bounds__(256)
                 const double* ar = Ainv + sp * S;
                 for (int64_t j = lane; j < S; j += 32) oa = fma(om[j], ar[j], oa);
                 oa = warp_sum(oa);
+            }
+            if (keepD) g += dirty[m] * s[sp];
+            if (keepF) g -= oms * s[sp] + oa;
+        }
+        if (lane == 0) grad[m * B + b] = g;
+    }
+}
+
+// The same gradient on the mixed path, from the double-float planes of Omega
+// (M x S) and A^-1 (S x S) and of s: the dot products run as double-float on
+// the float32 pipe, with no float64 copies of Omega or A^-1.
+__global__ void __launch_bounds__(256)
+    weight_grad_df_kernel(const int64_t* __restrict__ idx, int64_t M, int64_t B, int64_t S,
+                          const float* __restrict__ Omh, const float* __restrict__ Oml, const float* __restrict__ AIh,
+                          const float* __restrict__ AIl, const float* __restrict__ sh, const float* __restrict__ sl,
+                          const double* __restrict__ s, const double* __restrict__ dirty, int compact_mode,
+                          double* __restrict__ grad) {
+    const int lane = threadIdx.x & 31;
+    const int64_t m = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (m >= M) return;
+    const float* oh = Omh + m * S;
+    const float* ol = Oml + m * S;
+    df acc = {0.f, 0.f};
+    for (int64_t j = lane; j < S; j += 32) df_fma_acc(acc, {oh[j], ol[j]}, {sh[j], sl[j]});
+    const double oms = warp_sum(df_to(acc));
+    const int64_t* row = idx + m * B;
+    bool ended = false;
+    for (int64_t b = 0; b < B; ++b) {
+        const int64_t sp = row[b];
+        if (sp == -1) ended = true;
+        double g = 0.0;
+        if (!ended && sp >= 0 && sp < S) {
+            bool last = true;  // not overwritten by a later entry (dense-mapping semantics)
+            for (int64_t q = b + 1; q < B; ++q) {
+                if (row[q] == -1) break;
+                if (row[q] == sp) last = false;
+            }
+            const bool keepD = last;
+            const bool keepF = compact_mode ? true : last;
+            double oa = 0.0;
+            if (keepF) {
+                const float* ah = AIh + sp * S;
+                const float* al = AIl + sp * S;
+                df a = {0.f, 0.f};
+                for (int64_t j = lane; j < S; j += 32) df_fma_acc(a, {oh[j], ol[j]}, {ah[j], al[j]});
+                oa = warp_sum(df_to(a));
             }
             if (keepD) g += dirty[m] * s[sp];
             if (keepF) g -= oms * s[sp] + oa;
@@ -263,7 +316,7 @@ struct EvidenceBufs {
     DfSpd da{}, dh{};                 // mixed path
     double *TW, *Om, *F, *H, *A, *Ainv, *D, *s, *res, *kpart, *fpart, *logdets;
     float *Wh, *Wl;                   // w_tilde planes when split per call
-    float *TWh, *TWl, *Omh, *Oml, *Fh, *Fl, *Hh, *Hl, *Ah, *Al, *AIh, *AIl;
+    float *TWh, *TWl, *Omh, *Oml, *Fh, *Fl, *Hh, *Hl, *Ah, *Al, *AIh, *AIl, *sh, *sl;
     int64_t nk_blocks, nfrob;
     bool compact, grad, mixed;
 };
@@ -341,8 +394,8 @@ size_t evidence_carve(const aj_problem* p, bool mixed, bool with_grad, void* bas
         if (with_grad) {
             b.AIh = cv.take<float>(S * S);
             b.AIl = cv.take<float>(S * S);
-            b.Ainv = cv.take<double>(S * S);
-            b.Om = cv.take<double>(M * S);
+            b.sh = cv.take<float>(S);
+            b.sl = cv.take<float>(S);
         }
     }
     return align_up(cv.used);
@@ -446,7 +499,8 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         const float* fl[2] = {b.Al, b.Hl};
         DfSpd* fw[2] = {&b.da, &b.dh};
         double* ld[2] = {b.logdets + 0, b.logdets + 1};
-        AJ_TRY(dfspd_factor_invert_n(fh, fl, 2, with_grad ? 2 : 1, S, fw, ld, info, st));
+        AJ_TRY(dfspd_factor_invert_n(fh, fl, 2, with_grad ? 2 : 1, S, fw, ld, info, st, with_grad ? b.AIh : nullptr,
+                                     with_grad ? b.AIl : nullptr));
         AJ_TRY(dfspd_solve_refined(S, b.da, b.Ah, b.Al, b.D, b.s, b.res, st));
     }
 
@@ -473,17 +527,22 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         frob_lower_kernel<<<(unsigned)b.nfrob, 256, 0, st>>>(b.wh.Linv, S, b.fpart);
         AJ_LAUNCHED();
     } else {
-        AJ_TRY(dfspd_inverse_from_factor(S, b.da, b.AIh, b.AIl, st));
-        AJ_TRY(df_join(b.AIh, b.AIl, S * S, b.Ainv, st));
-        AJ_TRY(df_join(b.Omh, b.Oml, M * S, b.Om, st));
+        AJ_TRY(df_split(b.s, S, b.sh, b.sl, st));
         AJ_TRY(df_frob_lower(b.dh.Ih, b.dh.Il, S, b.fpart, b.nfrob, st));
     }
-    dlam_kernel<<<1, 1024, 0, st>>>(p->neighbors, p->neighbors_sizes, S, p->P, b.s, b.Ainv, b.fpart, b.nfrob,
+    dlam_kernel<<<1, 1024, 0, st>>>(p->neighbors, p->neighbors_sizes, S, p->P, b.s, mixed ? nullptr : b.Ainv, b.AIh,
+                                    b.AIl, b.fpart, b.nfrob,
                                     p->coefficient, p->coefficient_dev, mixed ? b.logdets + 4 : nullptr, out);
     AJ_LAUNCHED();
     if (M > 0 && B > 0) {
-        weight_grad_kernel<<<blocks_for(M * 32, 256), 256, 0, st>>>(p->pix_indexes, M, B, S, b.Om, b.Ainv, b.s,
-                                                                    p->dirty_image, b.compact ? 1 : 0, grad_weights);
+        if (mixed)
+            weight_grad_df_kernel<<<blocks_for(M * 32, 256), 256, 0, st>>>(
+                p->pix_indexes, M, B, S, b.Omh, b.Oml, b.AIh, b.AIl, b.sh, b.sl, b.s, p->dirty_image,
+                b.compact ? 1 : 0, grad_weights);
+        else
+            weight_grad_kernel<<<blocks_for(M * 32, 256), 256, 0, st>>>(p->pix_indexes, M, B, S, b.Om, b.Ainv, b.s,
+                                                                        p->dirty_image, b.compact ? 1 : 0,
+                                                                        grad_weights);
         AJ_LAUNCHED();
     }
     return AJ_OK;

@@ -31,6 +31,8 @@ struct DfMats {
     float* Il[2];
     float* dh[2];
     float* dl[2];
+    float* fh[2];  // factored diagonal blocks (copied into L after the last panel)
+    float* fl[2];
     double* piv[2];
     int ninv;  // matrices z < ninv also get L^-1: the panel writes its diagonal block
 };
@@ -284,8 +286,10 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 // -------------------------------------------------------------- Cholesky
 
 // Factor + invert the diagonal block at k0 (every block, redundantly), then:
-// block 0 stores L_kk, its inverse and the pivots; block b >= 1 replaces the
-// 64 panel rows k0 + 32 + 64 (b - 1) .. by A_rows L_kk^-T.
+// block 0 stores L_kk (in the factored-block buffer, not in L: blocks of the
+// same launch may start late and must still read the unfactored block from
+// L), its inverse and the pivots; block b >= 1 replaces the 64 panel rows
+// k0 + 32 + 64 (b - 1) .. by A_rows L_kk^-T.
 // Latency matters more than work here (one launch per 32 columns sits on the
 // critical path), so the kernel keeps its barrier count and its per-warp
 // instruction count low:
@@ -305,6 +309,8 @@ __global__ void __launch_bounds__(PANEL_THREADS)
     const int64_t kb = k0 / DNB;
     float* __restrict__ dh = pick(mats.dh, z) + kb * DNB * DNB;
     float* __restrict__ dl = pick(mats.dl, z) + kb * DNB * DNB;
+    float* __restrict__ fh = pick(mats.fh, z) + kb * DNB * DNB;
+    float* __restrict__ fl = pick(mats.fl, z) + kb * DNB * DNB;
     double* __restrict__ piv = pick(mats.piv, z);
     __shared__ float ah[DNB][DNB + 1], al[DNB][DNB + 1];
     __shared__ float ih[DNB][DNB + 1], il[DNB][DNB + 1];
@@ -423,15 +429,13 @@ __global__ void __launch_bounds__(PANEL_THREADS)
         float* __restrict__ Il = z < mats.ninv ? pick(mats.Il, z) : nullptr;
         for (int e = tid; e < DNB * DNB; e += PANEL_THREADS) {
             const int i = e / DNB, j = e % DNB;
-            if (i < nb && j < nb) {
+            if (Ih && i < nb && j < nb) {
                 const int64_t off = (k0 + i) * S + k0 + j;
-                Lh[off] = j <= i ? lh[i][j] : 0.f;
-                Ll[off] = j <= i ? ll[i][j] : 0.f;
-                if (Ih) {
-                    Ih[off] = ih[i][j];
-                    Il[off] = il[i][j];
-                }
+                Ih[off] = ih[i][j];
+                Il[off] = il[i][j];
             }
+            fh[e] = j <= i ? lh[i][j] : 0.f;
+            fl[e] = j <= i ? ll[i][j] : 0.f;
             dh[e] = ih[i][j];
             dl[e] = il[i][j];
         }
@@ -550,6 +554,22 @@ __global__ void __launch_bounds__(128)
         }
 }
 
+// L's diagonal blocks from the factored-block buffer; grid (blocks, matrices)
+__global__ void df_store_diag_kernel(DfMats mats, int64_t S) {
+    float* __restrict__ Lh = pick(mats.Lh, blockIdx.y);
+    float* __restrict__ Ll = pick(mats.Ll, blockIdx.y);
+    const float* __restrict__ fh = pick(mats.fh, blockIdx.y);
+    const float* __restrict__ fl = pick(mats.fl, blockIdx.y);
+    const int64_t kb = blockIdx.x, k0 = kb * DNB;
+    for (int e = threadIdx.x; e < DNB * DNB; e += blockDim.x) {
+        const int i = e / DNB, j = e % DNB;
+        if (k0 + i < S && k0 + j < S) {
+            Lh[(k0 + i) * S + k0 + j] = fh[kb * DNB * DNB + e];
+            Ll[(k0 + i) * S + k0 + j] = fl[kb * DNB * DNB + e];
+        }
+    }
+}
+
 __global__ void df_zero_upper_kernel(float* __restrict__ h, float* __restrict__ l, int64_t S) {
     for (int64_t i = blockIdx.y; i < S; i += gridDim.y)
         for (int64_t j = i + 1 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < S;
@@ -648,6 +668,69 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Streaming A^-1 = X^T X (X = L^-1 lower): once block row R of X is final,
+// add its contribution X[R][I]^T X[R][J] to every lower tile (I, J), J <= I <= R.
+// Summed over R this is the whole product, so A^-1 builds up while the
+// factorisation and L^-1 are still running instead of after them.  128
+// threads, 8 outputs each (the trailing-update layout).
+__global__ void __launch_bounds__(128)
+    df_lauum_row_kernel(const float* __restrict__ Xh, const float* __restrict__ Xl, float* __restrict__ Ch,
+                        float* __restrict__ Cl, int64_t S, int64_t R) {
+    __shared__ float pih[32][33], pil[32][33], pjh[32][33], pjl[32][33];
+    int64_t ti, tj;
+    lower_tile_df(blockIdx.x, ti, tj);
+    const int64_t r0 = R * DNB, i0 = ti * DNB, j0 = tj * DNB;
+    const int tid = threadIdx.x;
+    const int ty = tid >> 3, tx = tid & 7;  // outputs (i0 + ty + 16 a, j0 + tx + 8 b)
+    df cur[2][4];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int64_t gi = i0 + ty + 16 * a, gj = j0 + tx + 8 * b;
+            const bool in = gi < S && gj < S;
+            cur[a][b] = in ? df{Ch[gi * S + gj], Cl[gi * S + gj]} : df{0.f, 0.f};
+        }
+    // pi[c][x] = X[r0 + c][i0 + x], pj[c][x] = X[r0 + c][j0 + x]
+    for (int e = tid; e < 32 * 32; e += 128) {
+        const int c = e >> 5, x = e & 31;
+        const int64_t r = r0 + c;
+        const bool ii = r < S && i0 + x < S, jj = r < S && j0 + x < S;
+        pih[c][x] = ii ? Xh[r * S + i0 + x] : 0.f;
+        pil[c][x] = ii ? Xl[r * S + i0 + x] : 0.f;
+        pjh[c][x] = jj ? Xh[r * S + j0 + x] : 0.f;
+        pjl[c][x] = jj ? Xl[r * S + j0 + x] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c8 = 0; c8 < 32; c8 += 8) {
+#pragma unroll
+        for (int c = c8; c < c8 + 8; ++c) {
+            const df x0 = {pih[c][ty], pil[c][ty]}, x1 = {pih[c][ty + 16], pil[c][ty + 16]};
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const df y = {pjh[c][tx + 8 * b], pjl[c][tx + 8 * b]};
+                df_fma_lazy(cur[0][b], x0, y);
+                df_fma_lazy(cur[1][b], x1, y);
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) df_renorm(cur[a][b]);
+    }
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int64_t gi = i0 + ty + 16 * a, gj = j0 + tx + 8 * b;
+            if (gi < S && gj < S) {
+                Ch[gi * S + gj] = cur[a][b].hi;
+                Cl[gi * S + gj] = cur[a][b].lo;
+            }
+        }
+}
+
 __global__ void df_mirror_lower_kernel(float* __restrict__ h, float* __restrict__ l, int64_t S) {
     for (int64_t i = blockIdx.y; i < S; i += gridDim.y)
         for (int64_t j = i + 1 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < S;
@@ -657,35 +740,44 @@ __global__ void df_mirror_lower_kernel(float* __restrict__ h, float* __restrict_
         }
 }
 
-// y = op(Li) x for lower-triangular Li (double-float), x and y float64; one warp per output
+// y = op(Li) x for lower-triangular Li; x as double-float planes (converted
+// once, not per row), y float64 and, when yh is set, also as planes; one warp
+// per output
 __global__ void __launch_bounds__(256)
     df_trmv_kernel(const float* __restrict__ Lh, const float* __restrict__ Ll, int64_t S, int trans,
-                   const double* __restrict__ x, double* __restrict__ y) {
+                   const float* __restrict__ xh, const float* __restrict__ xl, double* __restrict__ y,
+                   float* __restrict__ yh, float* __restrict__ yl) {
     const int lane = threadIdx.x & 31;
     const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (i >= S) return;
     df acc = {0.f, 0.f};
     if (!trans) {
-        for (int64_t j = lane; j <= i; j += 32) df_fma_acc(acc, {Lh[i * S + j], Ll[i * S + j]}, df_from(x[j]));
+        for (int64_t j = lane; j <= i; j += 32) df_fma_acc(acc, {Lh[i * S + j], Ll[i * S + j]}, {xh[j], xl[j]});
     } else {
-        for (int64_t j = i + lane; j < S; j += 32) df_fma_acc(acc, {Lh[j * S + i], Ll[j * S + i]}, df_from(x[j]));
+        for (int64_t j = i + lane; j < S; j += 32) df_fma_acc(acc, {Lh[j * S + i], Ll[j * S + i]}, {xh[j], xl[j]});
     }
-    double v = df_to(acc);
-    v = warp_sum(v);
-    if (lane == 0) y[i] = v;
+    const double v = warp_sum(df_to(acc));
+    if (lane == 0) {
+        if (y) y[i] = v;
+        if (yh) {
+            const df d = df_from(v);
+            yh[i] = d.hi;
+            yl[i] = d.lo;
+        }
+    }
 }
 
-// r = b - A x for a full double-float A (x, b, r float64); one warp per row
+// r = b - A x for a full double-float A (x as planes; b, r float64); one warp per row
 __global__ void __launch_bounds__(256)
     df_residual_kernel(const float* __restrict__ Ah, const float* __restrict__ Al, int64_t S,
-                       const double* __restrict__ x, const double* __restrict__ b, double* __restrict__ r) {
+                       const float* __restrict__ xh, const float* __restrict__ xl, const double* __restrict__ b,
+                       double* __restrict__ r) {
     const int lane = threadIdx.x & 31;
     const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (i >= S) return;
     df acc = {0.f, 0.f};
-    for (int64_t j = lane; j < S; j += 32) df_fma_acc(acc, {Ah[i * S + j], Al[i * S + j]}, df_from(x[j]));
-    double v = df_to(acc);
-    v = warp_sum(v);
+    for (int64_t j = lane; j < S; j += 32) df_fma_acc(acc, {Ah[i * S + j], Al[i * S + j]}, {xh[j], xl[j]});
+    const double v = warp_sum(df_to(acc));
     if (lane == 0) r[i] = b[i] - v;
 }
 
@@ -715,8 +807,10 @@ size_t dfspd_bytes(int64_t S, bool with_inverse) {
     Sizer s;
     s.take<float>(2 * S * S);  // L planes
     if (with_inverse) s.take<float>(2 * S * S);
-    s.take<float>(2 * nbt * DNB * DNB);
+    s.take<float>(2 * nbt * DNB * DNB);  // diagonal-block inverses
+    s.take<float>(2 * nbt * DNB * DNB);  // factored diagonal blocks
     s.take<double>(S);  // pivots
+    s.take<double>(S);  // vector scratch
     s.take<double>(S);  // vector scratch
     return s.total();
 }
@@ -737,8 +831,12 @@ DfSpd dfspd_carve(Carver& cv, int64_t S, bool with_inverse) {
     float* d = cv.take<float>(2 * nbt * DNB * DNB);
     w.dh = d;
     w.dl = d ? d + nbt * DNB * DNB : nullptr;
+    float* f = cv.take<float>(2 * nbt * DNB * DNB);
+    w.fh = f;
+    w.fl = f ? f + nbt * DNB * DNB : nullptr;
     w.piv = cv.take<double>(S);
     w.vec = cv.take<double>(S);
+    w.vec2 = cv.take<double>(S);
     return w;
 }
 
@@ -773,6 +871,8 @@ static DfMats mats_of(DfSpd* const* w, int count) {
         m.Il[z] = x->Il;
         m.dh[z] = x->dh;
         m.dl[z] = x->dl;
+        m.fh[z] = x->fh;
+        m.fl[z] = x->fl;
         m.piv[z] = x->piv;
     }
     return m;
@@ -789,9 +889,11 @@ static DfMats mats_of(DfSpd* const* w, int count) {
 // k of L and the diagonal inverse of block k + 1, both final once panel k + 1
 // is done, so it trails the factorisation by one panel.
 int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int count, int n_inverse, int64_t S,
-                          DfSpd* const* w, double* const* logdet, int* info, cudaStream_t st) {
+                          DfSpd* const* w, double* const* logdet, int* info, cudaStream_t st, float* AIh,
+                          float* AIl) {
     if (S <= 0) return AJ_OK;
     if (count < 1 || count > 2 || n_inverse < 0 || n_inverse > count) return AJ_ERR_ARG;
+    if ((AIh || AIl) && (!AIh || !AIl || n_inverse < 1)) return AJ_ERR_ARG;
     dim3 zg(blocks_for(S, 256, 8), (unsigned)(S < 65535 ? S : 65535));
     for (int z = 0; z < count; ++z) {
         if (Ah[z] != w[z]->Lh) {
@@ -807,6 +909,9 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
         if (!w[z]->Ih) return AJ_ERR_ARG;
         if (cudaMemsetAsync(w[z]->Ih, 0, sizeof(float) * 2 * S * S, st) != cudaSuccess) return AJ_ERR_CUDA;
     }
+    if (AIh && (cudaMemsetAsync(AIh, 0, sizeof(float) * S * S, st) != cudaSuccess ||
+                cudaMemsetAsync(AIl, 0, sizeof(float) * S * S, st) != cudaSuccess))
+        return AJ_ERR_CUDA;
     DfMats m = mats_of(w, count);
     m.ninv = n_inverse;
     Lanes* lanes = nullptr;
@@ -823,7 +928,14 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
         dfchol_panel_kernel<<<dim3(g, count), PANEL_THREADS, 0, crit>>>(m, S, k0, info);
         return check_launch();
     };
+    // A^-1 of matrix 0, one final block row of its L^-1 at a time
+    auto lauum_row = [&](int64_t R, cudaStream_t on) {
+        const int64_t tiles = (R + 1) * (R + 2) / 2;
+        df_lauum_row_kernel<<<(unsigned)tiles, 128, 0, on>>>(w[0]->Ih, w[0]->Il, AIh, AIl, S, R);
+        return check_launch();
+    };
     AJ_TRY(panel(0));
+    if (AIh && nbt == 1) AJ_TRY(lauum_row(0, crit));
     for (int64_t kb = 0; kb + 1 < nbt; ++kb) {
         const int64_t k0 = kb * DNB;
         const int64_t tb = (S - k0 - DNB + 31) / 32;  // trailing tile rows (>= 1 here)
@@ -843,37 +955,40 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
             const int64_t tiles = (nbt - kb - 1) * (kb + 1);
             df_trtri_step_kernel<<<dim3((unsigned)tiles, n_inverse), 256, 0, tri>>>(m, S, kb);
             AJ_LAUNCHED();
+            // block row 0 of L^-1 is final since panel 0, block row kb + 1 after this step
+            if (AIh && kb == 0) AJ_TRY(lauum_row(0, tri));
+            if (AIh) AJ_TRY(lauum_row(kb + 1, tri));
         }
         if (tb > 1) AJ_TRY(lane_wait(ln, 0, kEvUpdate));
     }
+    df_store_diag_kernel<<<dim3((unsigned)nbt, count), 256, 0, crit>>>(m, S);
+    AJ_LAUNCHED();
     for (int z = 0; z < count; ++z)
         if (logdet && logdet[z]) {
             df_logdet_kernel<<<1, 1024, 0, crit>>>(w[z]->piv, S, logdet[z], info);
             AJ_LAUNCHED();
         }
-    return lanes_join(ln, st, nlanes);
+    AJ_TRY(lanes_join(ln, st, nlanes));
+    return AIh ? df_mirror_lower(AIh, AIl, S, st) : AJ_OK;
 }
 
 int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* logdet, int* info, cudaStream_t st) {
     DfSpd* ws[1] = {&w};
     double* ld[1] = {logdet};
-    return dfspd_factor_invert_n(&Ah, &Al, 1, 0, S, ws, ld, info, st);
+    return dfspd_factor_invert_n(&Ah, &Al, 1, 0, S, ws, ld, info, st, nullptr, nullptr);
 }
 
-int dfspd_inverse_from_factor(int64_t S, DfSpd& w, float* Ah, float* Al, cudaStream_t st) {
-    AJ_TRY(gemm_df(true, false, S, S, S, false, w.Ih, w.Il, S, w.Ih, w.Il, S, false, Ah, Al, S, true, true, st));
-    dim3 g(blocks_for(S, 256, 8), (unsigned)(S < 65535 ? S : 65535));
-    df_mirror_lower_kernel<<<g, 256, 0, st>>>(Ah, Al, S);
-    return check_launch();
-}
-
-// x = A^-1 b = Li^T (Li b) with the inverse factor
+// x = A^-1 b = Li^T (Li b) with the inverse factor; b and x may alias.  The
+// scratch vectors hold b's and Li b's planes (S hi floats, then S lo floats).
 int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st) {
     if (!w.Ih) return AJ_ERR_ARG;
+    float* bh = reinterpret_cast<float*>(w.vec);
+    float* uh = reinterpret_cast<float*>(w.vec2);
+    AJ_TRY(df_split(b, S, bh, bh + S, st));
     const unsigned g = blocks_for(S * 32, 256);
-    df_trmv_kernel<<<g, 256, 0, st>>>(w.Ih, w.Il, S, 0, b, w.vec);
+    df_trmv_kernel<<<g, 256, 0, st>>>(w.Ih, w.Il, S, 0, bh, bh + S, nullptr, uh, uh + S);
     AJ_LAUNCHED();
-    df_trmv_kernel<<<g, 256, 0, st>>>(w.Ih, w.Il, S, 1, w.vec, x);
+    df_trmv_kernel<<<g, 256, 0, st>>>(w.Ih, w.Il, S, 1, uh, uh + S, x, nullptr, nullptr);
     return check_launch();
 }
 
@@ -882,7 +997,9 @@ int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, c
                         cudaStream_t st) {
     AJ_TRY(dfspd_solve_vec(S, w, b, x, st));
     const unsigned g = blocks_for(S * 32, 256);
-    df_residual_kernel<<<g, 256, 0, st>>>(Ah, Al, S, x, b, r);
+    float* xh = reinterpret_cast<float*>(w.vec);
+    AJ_TRY(df_split(x, S, xh, xh + S, st));
+    df_residual_kernel<<<g, 256, 0, st>>>(Ah, Al, S, xh, xh + S, b, r);
     AJ_LAUNCHED();
     AJ_TRY(dfspd_solve_vec(S, w, r, r, st));
     add_vec_kernel<<<blocks_for(S, 256, 64), 256, 0, st>>>(x, r, S);
@@ -926,8 +1043,7 @@ int aj_spd_inverse_mixed(const double* A, int64_t S, double* Ainv, double* logde
     const float* al[1] = {Ap + S * S};
     DfSpd* ws[1] = {&w};
     double* ld[1] = {logdet};
-    AJ_TRY(dfspd_factor_invert_n(ah, al, 1, 1, S, ws, ld, info, st));
-    AJ_TRY(dfspd_inverse_from_factor(S, w, Ip, Ip + S * S, st));
+    AJ_TRY(dfspd_factor_invert_n(ah, al, 1, 1, S, ws, ld, info, st, Ip, Ip + S * S));
     return df_join(Ip, Ip + S * S, S * S, Ainv, st);
 }
 
