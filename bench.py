@@ -232,9 +232,10 @@ def time_region(fn, steps: int, dist: Dist, name: str = "region") -> float:
 
 # DRAM bytes (read + write) of one aj_spd_inverse_mixed call at S = 1,500, summed
 # over its launches, from the ncu capture in
-# profiles/spd_inverse_mixed_s1500_traffic.md (the group is L2-resident: its
-# working set, 7 float planes of S x S, is 63 MB).
-ROOFLINE_TRAFFIC_BYTES = None
+# profiles/spd_inverse_mixed_s1500_traffic.md.  ncu flushes L2 before every
+# launch, so this is cold-cache traffic, an upper bound: the group's working set
+# (7 double-float S x S planes, 63 MB) is L2-resident in a real replay.
+ROOFLINE_TRAFFIC_BYTES = 595e6
 
 
 def roofline(A, dist: Dist):
@@ -540,7 +541,10 @@ def wtilde_bench(d, dev, fp32_peak) -> dict:
     terms = M * (M + 1) / 2 * Ks
     fp32_flops = terms * 2 * 11.4 * 2
     return {"precision": "mixed (float64 panel, double-float product)", "K_sample": Ks, "M": M, "seconds": sec,
-            "terms_per_s": terms / sec, "fp32_pipe_frac": fp32_flops / sec / 1e12 / fp32_peak}
+            "terms_per_s": terms / sec, "fp32_pipe_frac": fp32_flops / sec / 1e12 / fp32_peak,
+            "fp32_pipe_frac_note": "double-float arithmetic only (22.8 float32 instructions per term); ncu measures "
+                                   "the product kernel's FMA pipe at 74.5% active "
+                                   "(profiles/w_tilde_mixed_m5024_full.md)"}
 
 
 def stage_times(d, w_tilde, dev, dist) -> dict:
