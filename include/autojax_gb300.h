@@ -16,8 +16,9 @@
  *     caller's device word `info` (0 = fine; see AJ_INFO_*), like cuSOLVER's
  *     devInfo; the caller reads it after the stream work completes;
  *   - `precision` selects AJ_FP64 (IEEE float64 throughout, the parity path)
- *     or AJ_MIXED (FP64 phase reduction and factorisations, FP32 cos sums with
- *     compensated accumulation and FP32 contractions).
+ *     or AJ_MIXED (float64 phase reduction, pivot logarithms and final sums;
+ *     the products, factorisations and inverses in double-float arithmetic,
+ *     hi + lo float32 pairs with ~2^-47 rounding, on the float32 pipe).
  *
  * Each declaration names the function of ickc/python-autojax it replaces
  * (file:line in src/autojax/).
@@ -41,6 +42,7 @@ extern "C" {
 #define AJ_INFO_OK 0
 #define AJ_INFO_INDEX_RANGE 1       /* an index was outside [0, n) and not -1 */
 #define AJ_INFO_NOT_POSITIVE_DEFINITE 2 /* Cholesky met a pivot <= 0 or NaN */
+#define AJ_INFO_TIMEOUT 3           /* a bounded wait inside a kernel ran out (the kernel stopped cleanly) */
 
 #define AJ_FP64 0
 #define AJ_MIXED 1

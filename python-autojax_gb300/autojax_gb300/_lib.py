@@ -21,6 +21,7 @@ AJ_NOALLOC_SOLVE_MAX_S = 1024
 AJ_BATCH_BRANCHES = 16
 AJ_INFO_INDEX_RANGE = 1
 AJ_INFO_NOT_POSITIVE_DEFINITE = 2
+AJ_INFO_TIMEOUT = 3
 AJ_FP64 = 0
 AJ_MIXED = 1
 

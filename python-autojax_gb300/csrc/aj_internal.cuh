@@ -37,8 +37,19 @@ int spd_inverse_from_factor(int64_t S, SpdWorkspace& w, double* Ainv, cudaStream
 
 // ---- lanes.cu (side streams that fork from and join back into the caller's stream)
 
-constexpr int kLaneCount = 3;  // 0: critical chain (highest priority), 1: bulk updates, 2: triangular inverse
-enum LaneEvent { kEvFork = 0, kEvPanel, kEvUpdate, kEvDiag, kEvJoin0, kLaneEvents = kEvJoin0 + kLaneCount };
+// 0: critical chain (highest priority), 1: bulk updates, 2: triangular inverse
+// (and A^-1) of the first matrix, 3: triangular inverse of the second
+constexpr int kLaneCount = 4;
+enum LaneEvent {
+    kEvFork = 0,
+    kEvPanel,
+    kEvUpdate,
+    kEvDiag,
+    kEvPre,      // the evaluation's independent pre-work forks here ...
+    kEvPreDone,  // ... and is joined here
+    kEvJoin0,
+    kLaneEvents = kEvJoin0 + kLaneCount
+};
 struct Lanes {
     cudaStream_t s[kLaneCount];
     cudaEvent_t ev[kLaneEvents];
@@ -81,9 +92,11 @@ int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* 
 int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int count, int n_inverse, int64_t S,
                           DfSpd* const* w, double* const* logdet, int* info, cudaStream_t st, float* AIh = nullptr,
                           float* AIl = nullptr);
-int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st);
+// x = A^-1 b through A^-1's planes (full) when given, else through the inverse factor
+int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st, const float* AIh = nullptr,
+                    const float* AIl = nullptr);
 int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x, double* r,
-                        cudaStream_t st);
+                        cudaStream_t st, const float* AIh = nullptr, const float* AIl = nullptr);
 int df_frob_lower(const float* h, const float* l, int64_t S, double* partial, int64_t nparts, cudaStream_t st);
 
 // ---- mapping.cu
@@ -113,7 +126,7 @@ int csc_spmm_t(const Csc& c, int64_t S, const Tin* X, int64_t ld_x, int64_t cols
                cudaStream_t st);
 // double-float planes: out (S x cols) = T^T X with X given as (hi, lo) planes
 int csc_spmm_t_df(const Csc& c, int64_t S, const float* Xh, const float* Xl, int64_t ld_x, int64_t cols, float* Oh,
-                  float* Ol, int64_t ld_out, cudaStream_t st);
+                  float* Ol, int64_t ld_out, int* info, cudaStream_t st);
 // out[s] = sum_e val[e] * x[row[e]]
 int csc_spmv_t(const Csc& c, int64_t S, const double* x, double* out, cudaStream_t st);
 // TW (S x M) with TW[s][m1] = sum_e val[e] * Wc(m1, row[e]) from the compact table (T float or double)

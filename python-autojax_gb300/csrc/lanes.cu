@@ -1,10 +1,10 @@
 // Side streams for work that forks from, and joins back into, the caller's stream.
 //
 // The blocked factorisations are chains of small, latency-bound launches.  They
-// run faster as three concurrent chains: the critical one (pivot panel, then
-// the next block column of the trailing update) on a high-priority stream, the
-// bulk of each trailing update on a low-priority one, and the triangular
-// inverse, which needs only finished panels, on a third.  Every fork starts
+// run faster as concurrent chains: the critical one (the pivot panels) on a
+// high-priority stream, the bulk of each trailing update on a low-priority
+// one, and the triangular inverses, which need only finished panels, on a
+// third and a fourth (one per matrix).  Every fork starts
 // with an event recorded on the caller's stream and every join ends with the
 // caller's stream waiting on each lane, so the caller sees one ordered stream,
 // and stream capture records the same dependencies as graph edges.
@@ -30,7 +30,8 @@ std::map<std::pair<int, cudaStream_t>, Lanes*> g_lanes;
 int create_lanes(Lanes& l) {
     int least = 0, greatest = 0;
     if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return AJ_ERR_CUDA;
-    const int prio[kLaneCount] = {greatest, least, greatest < least ? greatest + 1 : least};
+    const int mid = greatest < least ? greatest + 1 : least;
+    const int prio[kLaneCount] = {greatest, least, mid, mid};
     for (int i = 0; i < kLaneCount; ++i)
         if (cudaStreamCreateWithPriority(&l.s[i], cudaStreamNonBlocking, prio[i]) != cudaSuccess) return AJ_ERR_CUDA;
     for (int i = 0; i < kLaneEvents; ++i)

@@ -455,8 +455,48 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
     // sparse mapping: dense-mapping semantics for D (and for F of the w_tilde likelihood)
     AJ_TRY(csc_build(p->pix_indexes, p->pix_weights, nullptr, M, B, S, CSC_ASSIGN, b.ca, info, st));
     if (b.compact) AJ_TRY(csc_build(p->pix_indexes, p->pix_weights, nullptr, M, B, S, CSC_SUM, b.cs, info, st));
-    AJ_TRY(csc_spmv_t(b.ca, S, p->dirty_image, b.D, st));
-    AJ_TRY(regularization(p->coefficient, p->coefficient_dev, p->neighbors, p->neighbors_sizes, S, p->P, b.H, info, st));
+    // Work that does not depend on w_tilde runs on a side lane while the w_tilde
+    // products run here: D = T^T dirty, H (and its split, mixed), the chi^2 and
+    // log-noise sums.
+    Lanes* lanes = nullptr;
+    AJ_TRY(lanes_for(st, &lanes));
+    Lanes& ln = *lanes;
+    cudaStream_t pre = ln.s[2];
+    if (cudaEventRecord(ln.ev[kEvPre], st) != cudaSuccess || cudaStreamWaitEvent(pre, ln.ev[kEvPre], 0) != cudaSuccess)
+        return AJ_ERR_CUDA;
+    {
+        int rc = csc_spmv_t(b.ca, S, p->dirty_image, b.D, pre);
+        if (rc == AJ_OK)
+            rc = regularization(p->coefficient, p->coefficient_dev, p->neighbors, p->neighbors_sizes, S, p->P, b.H,
+                                info, pre);
+        if (rc == AJ_OK && mixed) {
+            laplacian_shift_kernel<<<1, 1024, 0, pre>>>(p->neighbors, p->neighbors_sizes, S, p->P, p->coefficient,
+                                                         p->coefficient_dev, b.logdets + 4);
+            rc = check_launch();
+            if (rc == AJ_OK) {
+                split_shifted_kernel<<<blocks_for(S * S, 256, 8 * num_sms()), 256, 0, pre>>>(b.H, S, b.logdets + 4,
+                                                                                             b.Hh, b.Hl);
+                rc = check_launch();
+            }
+        }
+        if (rc == AJ_OK) {
+            if (K > 0) {
+                k_terms_kernel<<<(unsigned)b.nk_blocks, KT_THREADS, 0, pre>>>(p->data, p->noise_map, 2 * K, b.kpart);
+                rc = check_launch();
+            } else if (cudaMemsetAsync(b.kpart, 0, sizeof(double) * 2 * b.nk_blocks, pre) != cudaSuccess) {
+                rc = AJ_ERR_CUDA;
+            }
+        }
+        // joined even after a failed enqueue, so st never runs ahead of the side lane
+        if (cudaEventRecord(ln.ev[kEvPreDone], pre) != cudaSuccess) return AJ_ERR_CUDA;
+        if (rc != AJ_OK) {
+            cudaStreamWaitEvent(st, ln.ev[kEvPreDone], 0);
+            return rc;
+        }
+    }
+    auto join_pre = [&]() {
+        return cudaStreamWaitEvent(st, ln.ev[kEvPreDone], 0) == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+    };
 
     if (!mixed) {
         // Omega = W T (via TW = T^T W, W symmetric), F = T^T Omega, A = F + H
@@ -466,6 +506,7 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
             AJ_TRY(csc_spmm_t<double, double>(b.cs, S, p->w_tilde64, M, M, b.TW, M, st));
         AJ_TRY(transpose<double>(b.TW, S, M, b.Om, st));
         AJ_TRY(csc_spmm_t<double, double>(b.cs, S, b.Om, S, S, b.F, S, st));
+        AJ_TRY(join_pre());
         add_kernel<<<blocks_for(S * S, 256, 8 * num_sms()), 256, 0, st>>>(b.F, b.H, b.A, S * S);
         AJ_LAUNCHED();
         AJ_TRY(spd_factor(b.A, S, b.wa, b.logdets + 0, info, st));
@@ -483,17 +524,13 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
                 Wh = b.Wh;
                 Wl = b.Wl;
             }
-            AJ_TRY(csc_spmm_t_df(b.cs, S, Wh, Wl, M, M, b.TWh, b.TWl, M, st));
+            AJ_TRY(csc_spmm_t_df(b.cs, S, Wh, Wl, M, M, b.TWh, b.TWl, M, info, st));
         }
         AJ_TRY(transpose<float>(b.TWh, S, M, b.Omh, st));
         AJ_TRY(transpose<float>(b.TWl, S, M, b.Oml, st));
-        AJ_TRY(csc_spmm_t_df(b.cs, S, b.Omh, b.Oml, S, S, b.Fh, b.Fl, S, st));
+        AJ_TRY(csc_spmm_t_df(b.cs, S, b.Omh, b.Oml, S, S, b.Fh, b.Fl, S, info, st));
+        AJ_TRY(join_pre());
         AJ_TRY(df_add_f64(b.Fh, b.Fl, b.H, S * S, b.Ah, b.Al, st));
-        laplacian_shift_kernel<<<1, 1024, 0, st>>>(p->neighbors, p->neighbors_sizes, S, p->P, p->coefficient,
-                                                   p->coefficient_dev, b.logdets + 4);
-        AJ_LAUNCHED();
-        split_shifted_kernel<<<blocks_for(S * S, 256, 8 * num_sms()), 256, 0, st>>>(b.H, S, b.logdets + 4, b.Hh, b.Hl);
-        AJ_LAUNCHED();
         // A and H share every factorisation launch (and, with the gradient, every inversion launch)
         const float* fh[2] = {b.Ah, b.Hh};
         const float* fl[2] = {b.Al, b.Hl};
@@ -501,16 +538,11 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         double* ld[2] = {b.logdets + 0, b.logdets + 1};
         AJ_TRY(dfspd_factor_invert_n(fh, fl, 2, with_grad ? 2 : 1, S, fw, ld, info, st, with_grad ? b.AIh : nullptr,
                                      with_grad ? b.AIl : nullptr));
-        AJ_TRY(dfspd_solve_refined(S, b.da, b.Ah, b.Al, b.D, b.s, b.res, st));
+        AJ_TRY(dfspd_solve_refined(S, b.da, b.Ah, b.Al, b.D, b.s, b.res, st, with_grad ? b.AIh : nullptr,
+                                   with_grad ? b.AIl : nullptr));
     }
 
-    // chi.chi and sum log|noise| over the 2K reals, then logE
-    if (K > 0) {
-        k_terms_kernel<<<(unsigned)b.nk_blocks, KT_THREADS, 0, st>>>(p->data, p->noise_map, 2 * K, b.kpart);
-        AJ_LAUNCHED();
-    } else if (cudaMemsetAsync(b.kpart, 0, sizeof(double) * 2 * b.nk_blocks, st) != cudaSuccess) {
-        return AJ_ERR_CUDA;
-    }
+    // logE from the chi^2 and log-noise sums (side lane), s.D and the log-determinants
     assemble_kernel<<<1, 1024, 0, st>>>(b.kpart, b.nk_blocks, K, b.s, b.D, S, b.logdets, mixed ? b.logdets + 4 : nullptr,
                                         out);
     AJ_LAUNCHED();

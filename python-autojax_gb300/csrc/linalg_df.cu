@@ -299,10 +299,15 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 //    (inv [[A, 0], [B, C]] = [[A^-1, 0], [-C^-1 B A^-1, C^-1]]);
 //  - panel product: each warp owns two columns whose triangular dot-product
 //    lengths add to 33, so all lanes of a warp run the same loop.
+// With `pre` set the kernel first applies the previous step's update to its
+// own block column (A_kk -= P_k P_k^T, rows -= P_r P_k^T with P the previous
+// panel's rows), so the critical chain is one launch per step; the rest of
+// each trailing update runs on another lane.
 constexpr int PANEL_THREADS = 512;
+constexpr size_t PANEL_DYN_SMEM = sizeof(float) * 2 * 64 * (32 + 1);  // previous-panel rows of this block
 
 __global__ void __launch_bounds__(PANEL_THREADS)
-    dfchol_panel_kernel(DfMats mats, int64_t S, int64_t k0, int* info) {
+    dfchol_panel_kernel(DfMats mats, int64_t S, int64_t k0, int pre, int* info) {
     const int z = blockIdx.y;
     float* __restrict__ Lh = pick(mats.Lh, z);
     float* __restrict__ Ll = pick(mats.Ll, z);
@@ -318,9 +323,13 @@ __global__ void __launch_bounds__(PANEL_THREADS)
     __shared__ float rh[DNB], rl[DNB];
     __shared__ float th[DNB * DNB / 4], tl[DNB * DNB / 4];
     __shared__ float xh[64][DNB + 1], xl[64][DNB + 1];
+    extern __shared__ float panel_dyn[];
+    float(*prh)[DNB + 1] = reinterpret_cast<float(*)[DNB + 1]>(panel_dyn);
+    float(*prl)[DNB + 1] = reinterpret_cast<float(*)[DNB + 1]>(panel_dyn + 64 * (DNB + 1));
     __shared__ int bad;
     const int tid = threadIdx.x;
     const int64_t nb = (S - k0) < DNB ? (S - k0) : DNB;
+    const int64_t kp = k0 - DNB;  // the previous panel's first column (pre only)
     if (tid == 0) bad = 0;
     for (int e = tid; e < DNB * DNB; e += PANEL_THREADS) {
         const int i = e / DNB, j = e % DNB;
@@ -335,8 +344,10 @@ __global__ void __launch_bounds__(PANEL_THREADS)
         }
         ah[i][j] = vh;
         al[i][j] = vl;
-        ih[i][j] = 0.f;
-        il[i][j] = 0.f;
+        // with pre, ih/il first hold the previous panel's pivot-block rows P_k
+        const bool pin = pre && i < nb;
+        ih[i][j] = pin ? Lh[(k0 + i) * S + kp + j] : 0.f;
+        il[i][j] = pin ? Ll[(k0 + i) * S + kp + j] : 0.f;
         lh[i][j] = 0.f;
         ll[i][j] = 0.f;
     }
@@ -349,9 +360,46 @@ __global__ void __launch_bounds__(PANEL_THREADS)
             const bool in = r < S && j < nb;
             xh[i][j] = in ? Lh[r * S + k0 + j] : 0.f;
             xl[i][j] = in ? Ll[r * S + k0 + j] : 0.f;
+            if (pre) {
+                prh[i][j] = r < S ? Lh[r * S + kp + j] : 0.f;
+                prl[i][j] = r < S ? Ll[r * S + kp + j] : 0.f;
+            }
         }
     }
     __syncthreads();
+    if (pre) {
+        // A_kk (lower) -= P_k P_k^T and rows -= P_r P_k^T: element (i, j) sums p over the 32 previous columns
+        const int nout = DNB * DNB + (blockIdx.x > 0 ? 64 * DNB : 0);
+        for (int o = tid; o < nout; o += PANEL_THREADS) {
+            const bool diag = o < DNB * DNB;
+            const int i = diag ? o / DNB : (o - DNB * DNB) / DNB, j = o % DNB;
+            if (diag && j > i) continue;
+            df acc = {0.f, 0.f};
+#pragma unroll 8
+            for (int q = 0; q < DNB; ++q) {
+                const df x = diag ? df{ih[i][q], il[i][q]} : df{prh[i][q], prl[i][q]};
+                df_fma_lazy(acc, x, {ih[j][q], il[j][q]});
+                if ((q & 7) == 7) df_renorm(acc);
+            }
+            if (diag) {
+                if (i < nb && j < nb) {
+                    const df v = df_add({ah[i][j], al[i][j]}, df_neg(acc));
+                    ah[i][j] = v.hi;
+                    al[i][j] = v.lo;
+                }
+            } else {
+                const df v = df_add({xh[i][j], xl[i][j]}, df_neg(acc));
+                xh[i][j] = v.hi;
+                xl[i][j] = v.lo;
+            }
+        }
+        __syncthreads();
+        for (int e = tid; e < DNB * DNB; e += PANEL_THREADS) {
+            ih[e / DNB][e % DNB] = 0.f;
+            il[e / DNB][e % DNB] = 0.f;
+        }
+        __syncthreads();
+    }
     const int ur = tid >> 4, uq = tid & 15;  // update: row ur, columns uq and uq + 16
     // one barrier a column: every thread evaluates the pivot itself; the scaled
     // column goes to L (lh/ll) so the update can keep reading the unscaled one
@@ -472,31 +520,21 @@ __global__ void __launch_bounds__(PANEL_THREADS)
     }
 }
 
-// Trailing update of one Cholesky step: C (lower 32 x 32 tiles of the r x r
-// trailing matrix) -= P P^T with P the r x 32 solved panel.  128 threads, 8
-// outputs each; small register and shared footprint so several blocks share
-// an SM and the late, small steps still fill the GPU.  `part` selects the
-// tiles: all of them (UPD_ALL), the first tile column only (UPD_NEXT: the next
-// panel, on the critical path) or every other column (UPD_REST).
-enum UpdatePart { UPD_ALL = 0, UPD_NEXT = 1, UPD_REST = 2 };
-
+// Trailing update of one Cholesky step past the next block column (which the
+// next panel kernel updates itself): C (lower 32 x 32 tiles of the trailing
+// matrix, tile columns >= 1) -= P P^T with P the solved panel.  128 threads,
+// 8 outputs each; small register and shared footprint so several blocks share
+// an SM and the late, small steps still fill the GPU.
 __global__ void __launch_bounds__(128)
-    dfsyrk_update_kernel(DfMats mats, int64_t S, int64_t k0, int part) {
+    dfsyrk_update_kernel(DfMats mats, int64_t S, int64_t k0) {
     float* __restrict__ Lh = pick(mats.Lh, blockIdx.y);
     float* __restrict__ Ll = pick(mats.Ll, blockIdx.y);
     __shared__ float pih[32][33], pil[32][33], pjh[32][33], pjl[32][33];
     const int64_t r0 = k0 + DNB;
     int64_t ti, tj;
-    if (part == UPD_NEXT) {
-        ti = blockIdx.x;
-        tj = 0;
-    } else {
-        lower_tile_df(blockIdx.x, ti, tj);
-        if (part == UPD_REST) {
-            ++ti;
-            ++tj;
-        }
-    }
+    lower_tile_df(blockIdx.x, ti, tj);
+    ++ti;
+    ++tj;
     const int64_t i0 = r0 + ti * 32, j0 = r0 + tj * 32;
     const int tid = threadIdx.x;
     const int ty = tid >> 3, tx = tid & 7;  // rows ty, ty+16; columns tx, tx+8, tx+16, tx+24
@@ -740,45 +778,78 @@ __global__ void df_mirror_lower_kernel(float* __restrict__ h, float* __restrict_
         }
 }
 
-// y = op(Li) x for lower-triangular Li; x as double-float planes (converted
-// once, not per row), y float64 and, when yh is set, also as planes; one warp
-// per output
+// Output of a matrix-vector product: float64 and, when yh is set, double-float planes.
+__device__ __forceinline__ void store_y(double v, int64_t i, double* y, float* yh, float* yl) {
+    if (y) y[i] = v;
+    if (yh) {
+        const df d = df_from(v);
+        yh[i] = d.hi;
+        yl[i] = d.lo;
+    }
+}
+
+// y = Li x for lower-triangular Li; x as double-float planes (converted once,
+// not per row).  One warp per row, four independent accumulators per lane so
+// several loads are in flight.
 __global__ void __launch_bounds__(256)
-    df_trmv_kernel(const float* __restrict__ Lh, const float* __restrict__ Ll, int64_t S, int trans,
+    df_trmv_kernel(const float* __restrict__ Lh, const float* __restrict__ Ll, int64_t S,
                    const float* __restrict__ xh, const float* __restrict__ xl, double* __restrict__ y,
                    float* __restrict__ yh, float* __restrict__ yl) {
     const int lane = threadIdx.x & 31;
     const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (i >= S) return;
-    df acc = {0.f, 0.f};
-    if (!trans) {
-        for (int64_t j = lane; j <= i; j += 32) df_fma_acc(acc, {Lh[i * S + j], Ll[i * S + j]}, {xh[j], xl[j]});
-    } else {
-        for (int64_t j = i + lane; j < S; j += 32) df_fma_acc(acc, {Lh[j * S + i], Ll[j * S + i]}, {xh[j], xl[j]});
-    }
-    const double v = warp_sum(df_to(acc));
-    if (lane == 0) {
-        if (y) y[i] = v;
-        if (yh) {
-            const df d = df_from(v);
-            yh[i] = d.hi;
-            yl[i] = d.lo;
-        }
-    }
+    df acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    const float* rh = Lh + i * S;
+    const float* rl = Ll + i * S;
+    int64_t j = lane;
+    for (; j + 96 <= i; j += 128)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) df_fma_acc(acc[u], {rh[j + 32 * u], rl[j + 32 * u]}, {xh[j + 32 * u], xl[j + 32 * u]});
+    for (; j <= i; j += 32) df_fma_acc(acc[0], {rh[j], rl[j]}, {xh[j], xl[j]});
+    const double v = warp_sum(df_to(df_add(df_add(acc[0], acc[1]), df_add(acc[2], acc[3]))));
+    if (lane == 0) store_y(v, i, y, yh, yl);
 }
 
-// r = b - A x for a full double-float A (x as planes; b, r float64); one warp per row
+// y = Li^T x: y[i] = sum_{j >= i} Li[j][i] x[j]; one warp per output, lanes
+// over the rows j (column access: the path without A^-1 uses it twice per solve)
 __global__ void __launch_bounds__(256)
-    df_residual_kernel(const float* __restrict__ Ah, const float* __restrict__ Al, int64_t S,
-                       const float* __restrict__ xh, const float* __restrict__ xl, const double* __restrict__ b,
-                       double* __restrict__ r) {
+    df_trmv_t_kernel(const float* __restrict__ Lh, const float* __restrict__ Ll, int64_t S,
+                     const float* __restrict__ xh, const float* __restrict__ xl, double* __restrict__ y,
+                     float* __restrict__ yh, float* __restrict__ yl) {
     const int lane = threadIdx.x & 31;
     const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (i >= S) return;
-    df acc = {0.f, 0.f};
-    for (int64_t j = lane; j < S; j += 32) df_fma_acc(acc, {Ah[i * S + j], Al[i * S + j]}, {xh[j], xl[j]});
-    const double v = warp_sum(df_to(acc));
-    if (lane == 0) r[i] = b[i] - v;
+    df acc[2] = {{0.f, 0.f}, {0.f, 0.f}};
+    int64_t j = i + lane;
+    for (; j + 32 < S; j += 64) {
+        df_fma_acc(acc[0], {Lh[j * S + i], Ll[j * S + i]}, {xh[j], xl[j]});
+        df_fma_acc(acc[1], {Lh[(j + 32) * S + i], Ll[(j + 32) * S + i]}, {xh[j + 32], xl[j + 32]});
+    }
+    for (; j < S; j += 32) df_fma_acc(acc[0], {Lh[j * S + i], Ll[j * S + i]}, {xh[j], xl[j]});
+    const double v = warp_sum(df_to(df_add(acc[0], acc[1])));
+    if (lane == 0) store_y(v, i, y, yh, yl);
+}
+
+// y = A x, or y = b - A x when b is set, for a full double-float A (x as
+// planes; b, y float64, y also as planes when yh is set); one warp per row,
+// four independent accumulators per lane
+__global__ void __launch_bounds__(256)
+    df_gemv_kernel(const float* __restrict__ Ah, const float* __restrict__ Al, int64_t S,
+                   const float* __restrict__ xh, const float* __restrict__ xl, const double* __restrict__ b,
+                   double* __restrict__ y, float* __restrict__ yh, float* __restrict__ yl) {
+    const int lane = threadIdx.x & 31;
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (i >= S) return;
+    df acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    const float* rh = Ah + i * S;
+    const float* rl = Al + i * S;
+    int64_t j = lane;
+    for (; j + 96 < S; j += 128)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) df_fma_acc(acc[u], {rh[j + 32 * u], rl[j + 32 * u]}, {xh[j + 32 * u], xl[j + 32 * u]});
+    for (; j < S; j += 32) df_fma_acc(acc[0], {rh[j], rl[j]}, {xh[j], xl[j]});
+    const double v = warp_sum(df_to(df_add(df_add(acc[0], acc[1]), df_add(acc[2], acc[3]))));
+    if (lane == 0) store_y(b ? b[i] - v : v, i, y, yh, yl);
 }
 
 __global__ void add_vec_kernel(double* __restrict__ x, const double* __restrict__ d, int64_t n) {
@@ -917,15 +988,36 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
     Lanes* lanes = nullptr;
     AJ_TRY(lanes_for(st, &lanes));
     Lanes& ln = *lanes;
-    const int nlanes = n_inverse > 0 ? 3 : 2;
+    const int nlanes = 2 + n_inverse;
     AJ_TRY(lanes_fork(ln, st, nlanes));
     cudaStream_t crit = ln.s[0], bulk = ln.s[1], tri = ln.s[2];
+    // each matrix's L^-1 on its own lane: a view of m whose slot 0 is matrix z
+    DfMats one[2] = {m, m};
+    for (int z = 0; z < 2; ++z) {
+        one[z].Lh[0] = one[z].Lh[1] = m.Lh[z];
+        one[z].Ll[0] = one[z].Ll[1] = m.Ll[z];
+        one[z].Ih[0] = one[z].Ih[1] = m.Ih[z];
+        one[z].Il[0] = one[z].Il[1] = m.Il[z];
+        one[z].dh[0] = one[z].dh[1] = m.dh[z];
+        one[z].dl[0] = one[z].dl[1] = m.dl[z];
+    }
     const int64_t nbt = (S + DNB - 1) / DNB;
+    static bool panel_attr[64] = {};
+    {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) return AJ_ERR_CUDA;
+        if (dev < 64 && !panel_attr[dev]) {
+            if (cudaFuncSetAttribute(dfchol_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)PANEL_DYN_SMEM) != cudaSuccess)
+                return AJ_ERR_CUDA;
+            panel_attr[dev] = true;
+        }
+    }
     auto panel = [&](int64_t kb) {
         const int64_t k0 = kb * DNB;
         const int64_t below = S - k0 - DNB;
         const unsigned g = 1 + (unsigned)(below > 0 ? (below + 63) / 64 : 0);
-        dfchol_panel_kernel<<<dim3(g, count), PANEL_THREADS, 0, crit>>>(m, S, k0, info);
+        dfchol_panel_kernel<<<dim3(g, count), PANEL_THREADS, PANEL_DYN_SMEM, crit>>>(m, S, k0, kb > 0 ? 1 : 0, info);
         return check_launch();
     };
     // A^-1 of matrix 0, one final block row of its L^-1 at a time
@@ -934,32 +1026,38 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
         df_lauum_row_kernel<<<(unsigned)tiles, 128, 0, on>>>(w[0]->Ih, w[0]->Il, AIh, AIl, S, R);
         return check_launch();
     };
+    // Step kb: panel kb + 1 applies panel kb's update to its own block column,
+    // so it only has to wait for the bulk update of step kb - 1 (which reached
+    // that column); the bulk update of step kb covers the columns after it.
     AJ_TRY(panel(0));
     if (AIh && nbt == 1) AJ_TRY(lauum_row(0, crit));
+    bool rest_prev = false;
     for (int64_t kb = 0; kb + 1 < nbt; ++kb) {
         const int64_t k0 = kb * DNB;
         const int64_t tb = (S - k0 - DNB + 31) / 32;  // trailing tile rows (>= 1 here)
-        dfsyrk_update_kernel<<<dim3((unsigned)tb, count), 128, 0, crit>>>(m, S, k0, UPD_NEXT);
-        AJ_LAUNCHED();
+        // wait for the previous bulk update before kEvUpdate is recorded again
+        if (rest_prev) AJ_TRY(lane_wait(ln, 0, kEvUpdate));
         if (tb > 1) {
             AJ_TRY(lane_signal(ln, kEvPanel, 0));
             AJ_TRY(lane_wait(ln, 1, kEvPanel));
-            dfsyrk_update_kernel<<<dim3((unsigned)((tb - 1) * tb / 2), count), 128, 0, bulk>>>(m, S, k0, UPD_REST);
+            dfsyrk_update_kernel<<<dim3((unsigned)((tb - 1) * tb / 2), count), 128, 0, bulk>>>(m, S, k0);
             AJ_LAUNCHED();
             AJ_TRY(lane_signal(ln, kEvUpdate, 1));
         }
+        rest_prev = tb > 1;
         AJ_TRY(panel(kb + 1));
         if (n_inverse > 0) {
             AJ_TRY(lane_signal(ln, kEvDiag, 0));
-            AJ_TRY(lane_wait(ln, 2, kEvDiag));
             const int64_t tiles = (nbt - kb - 1) * (kb + 1);
-            df_trtri_step_kernel<<<dim3((unsigned)tiles, n_inverse), 256, 0, tri>>>(m, S, kb);
-            AJ_LAUNCHED();
+            for (int z = 0; z < n_inverse; ++z) {
+                AJ_TRY(lane_wait(ln, 2 + z, kEvDiag));
+                df_trtri_step_kernel<<<(unsigned)tiles, 256, 0, ln.s[2 + z]>>>(one[z], S, kb);
+                AJ_LAUNCHED();
+            }
             // block row 0 of L^-1 is final since panel 0, block row kb + 1 after this step
             if (AIh && kb == 0) AJ_TRY(lauum_row(0, tri));
             if (AIh) AJ_TRY(lauum_row(kb + 1, tri));
         }
-        if (tb > 1) AJ_TRY(lane_wait(ln, 0, kEvUpdate));
     }
     df_store_diag_kernel<<<dim3((unsigned)nbt, count), 256, 0, crit>>>(m, S);
     AJ_LAUNCHED();
@@ -978,30 +1076,36 @@ int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* 
     return dfspd_factor_invert_n(&Ah, &Al, 1, 0, S, ws, ld, info, st, nullptr, nullptr);
 }
 
-// x = A^-1 b = Li^T (Li b) with the inverse factor; b and x may alias.  The
+// x = A^-1 b, b and x may alias.  With A^-1's planes (AIh/AIl, full) it is one
+// row-wise product; otherwise Li^T (Li b) with the inverse factor.  The
 // scratch vectors hold b's and Li b's planes (S hi floats, then S lo floats).
-int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st) {
-    if (!w.Ih) return AJ_ERR_ARG;
+int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st, const float* AIh,
+                    const float* AIl) {
     float* bh = reinterpret_cast<float*>(w.vec);
-    float* uh = reinterpret_cast<float*>(w.vec2);
     AJ_TRY(df_split(b, S, bh, bh + S, st));
     const unsigned g = blocks_for(S * 32, 256);
-    df_trmv_kernel<<<g, 256, 0, st>>>(w.Ih, w.Il, S, 0, bh, bh + S, nullptr, uh, uh + S);
+    if (AIh) {
+        df_gemv_kernel<<<g, 256, 0, st>>>(AIh, AIl, S, bh, bh + S, nullptr, x, nullptr, nullptr);
+        return check_launch();
+    }
+    if (!w.Ih) return AJ_ERR_ARG;
+    float* uh = reinterpret_cast<float*>(w.vec2);
+    df_trmv_kernel<<<g, 256, 0, st>>>(w.Ih, w.Il, S, bh, bh + S, nullptr, uh, uh + S);
     AJ_LAUNCHED();
-    df_trmv_kernel<<<g, 256, 0, st>>>(w.Ih, w.Il, S, 1, uh, uh + S, x, nullptr, nullptr);
+    df_trmv_t_kernel<<<g, 256, 0, st>>>(w.Ih, w.Il, S, uh, uh + S, x, nullptr, nullptr);
     return check_launch();
 }
 
 // x = A^-1 b with one step of iterative refinement against A (planes); r is S scratch
 int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x, double* r,
-                        cudaStream_t st) {
-    AJ_TRY(dfspd_solve_vec(S, w, b, x, st));
+                        cudaStream_t st, const float* AIh, const float* AIl) {
+    AJ_TRY(dfspd_solve_vec(S, w, b, x, st, AIh, AIl));
     const unsigned g = blocks_for(S * 32, 256);
     float* xh = reinterpret_cast<float*>(w.vec);
     AJ_TRY(df_split(x, S, xh, xh + S, st));
-    df_residual_kernel<<<g, 256, 0, st>>>(Ah, Al, S, xh, xh + S, b, r);
+    df_gemv_kernel<<<g, 256, 0, st>>>(Ah, Al, S, xh, xh + S, b, r, nullptr, nullptr);
     AJ_LAUNCHED();
-    AJ_TRY(dfspd_solve_vec(S, w, r, r, st));
+    AJ_TRY(dfspd_solve_vec(S, w, r, r, st, AIh, AIl));
     add_vec_kernel<<<blocks_for(S, 256, 64), 256, 0, st>>>(x, r, S);
     return check_launch();
 }
