@@ -343,6 +343,11 @@ def gpu_arm(args, dist: Dist) -> dict:
     mods = models(d)
     for e in ev.values():
         e.set_model(*mods[0][:4], coefficient=mods[0][4])
+    # tile shapes of the double-float factorisation, chosen by timing this evaluation
+    from autojax_gb300 import tune
+
+    tuned = tune.tune_tile_policy(ev["mixed"].launch)
+    for e in ev.values():
         if not args.no_graph:
             e.capture()
     coefs = [torch.full((1,), m[4], dtype=torch.float64, device=dev) for m in mods]
@@ -417,6 +422,9 @@ def gpu_arm(args, dist: Dist) -> dict:
             "l2": "inputs larger than L2 (w_tilde 722 MB float64 re-read every step)",
             "graph": not args.no_graph,
             "parallelism": f"replicas x{dist.world}",
+            "tile_policy": {"min_64_tiles (update, L^-1, A^-1)": list(tuned["policy"]),
+                            "tuned_ms": tuned["ms"], "default_ms": tuned["ms_default"],
+                            "candidates_timed": tuned["candidates_timed"]},
         },
         "fp64_path": {"value": args.steps * dist.world / t_fp64, "ms_per_step": 1e3 * t_fp64 / args.steps},
         "mixed_over_fp64": t_fp64 / t_mixed,

@@ -42,7 +42,6 @@ extern "C" {
 #define AJ_INFO_OK 0
 #define AJ_INFO_INDEX_RANGE 1       /* an index was outside [0, n) and not -1 */
 #define AJ_INFO_NOT_POSITIVE_DEFINITE 2 /* Cholesky met a pivot <= 0 or NaN */
-#define AJ_INFO_TIMEOUT 3           /* a bounded wait inside a kernel ran out (the kernel stopped cleanly) */
 
 #define AJ_FP64 0
 #define AJ_MIXED 1
@@ -112,6 +111,25 @@ size_t aj_w_tilde_data_workspace_size(int64_t M, int64_t K, int precision);
 int aj_w_tilde_data(const double* visibilities_real, const double* noise_map_real, const double* uv,
                     const double* grid_slim, int64_t K, int64_t M, double* out, void* workspace,
                     size_t workspace_bytes, int precision, void* stream);
+
+/* Tile policy of the double-float factorisation (no reference counterpart).
+ * A step of the trailing update, of L^-1 or of the streamed A^-1 runs in
+ * 64 x 64 output tiles when it has at least this many of them (per matrix),
+ * else in 32 x 32 tiles. Results do not depend on the choice; speed does.
+ * Process-wide; set between calls (a captured graph keeps the choice made at
+ * capture). autojax_gb300.tune picks the values by timing. */
+int aj_set_tile_policy(int update_min_tiles, int inverse_min_tiles, int lauum_min_tiles);
+int aj_get_tile_policy(int* out3);
+
+/* Dirty image (no reference function; the reference reads it from its
+ * dataset, tests.py:424-426): out[i] = sum_k noise_k^-2 (Re V_k cos t - Im V_k
+ * sin t), t = 2 pi (x_i u_k + y_i v_k), x = grid[:,1], y = grid[:,0]; the
+ * adjoint of the DFT, consistent with the chi^2 expansion the likelihood uses.
+ * visibilities (K,) complex128. Float64 throughout. */
+size_t aj_dirty_image_workspace_size(int64_t M, int64_t K);
+int aj_dirty_image(const double* visibilities, const double* noise_map_real, const double* uv,
+                   const double* grid_slim, int64_t K, int64_t M, double* out, void* workspace,
+                   size_t workspace_bytes, void* stream);
 
 /* numba.py:238-255 w_tilde_via_compact_from. out64/out32 (M, M), either may be NULL.
  * Offsets outside the table set info = AJ_INFO_INDEX_RANGE and write 0. */

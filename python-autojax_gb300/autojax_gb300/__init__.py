@@ -14,6 +14,7 @@ from .api import (  # noqa: F401
     curvature_matrix_via_w_tilde_from,
     curvature_matrix_via_w_wilde_sparse_mapping_matrix_from,
     data_vector_from,
+    dirty_image_from,
     log_evidence_and_grad,
     log_likelihood_function_via_w_compact_from,
     log_likelihood_function_via_w_tilde_from,

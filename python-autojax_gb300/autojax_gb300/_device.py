@@ -97,8 +97,6 @@ class Call:
             raise IndexError(f"{self.name}: index out of range (flat position {where})")
         if code == _lib.AJ_INFO_NOT_POSITIVE_DEFINITE:
             raise np.linalg.LinAlgError(f"{self.name}: matrix is not positive definite (pivot {where})")
-        if code == _lib.AJ_INFO_TIMEOUT:
-            raise RuntimeError(f"{self.name}: a bounded device wait ran out (block {where}); results are invalid")
 
     def out(self, t: torch.Tensor):
         return t.cpu().numpy() if self.numpy_out else t

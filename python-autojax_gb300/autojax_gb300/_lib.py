@@ -21,7 +21,6 @@ AJ_NOALLOC_SOLVE_MAX_S = 1024
 AJ_BATCH_BRANCHES = 16
 AJ_INFO_INDEX_RANGE = 1
 AJ_INFO_NOT_POSITIVE_DEFINITE = 2
-AJ_INFO_TIMEOUT = 3
 AJ_FP64 = 0
 AJ_MIXED = 1
 
@@ -102,6 +101,10 @@ SIGNATURES = {
     "aj_split_f64": (INT, [P, I64, P, P, P]),
     "aj_log_evidence_workspace_size": (SZ, [C.POINTER(Problem), INT, INT]),
     "aj_log_evidence": (INT, [C.POINTER(Problem), INT, INT, P, P, P, P, SZ, P, P]),
+    "aj_set_tile_policy": (INT, [INT, INT, INT]),
+    "aj_get_tile_policy": (INT, [P]),
+    "aj_dirty_image_workspace_size": (SZ, [I64, I64]),
+    "aj_dirty_image": (INT, [P, P, P, P, I64, I64, P, P, SZ, P]),
     "aj_sis_trace": (INT, [P, I64, D, P, P, P]),
     "aj_sis_trace_vjp": (INT, [P, I64, P, P, P]),
     "aj_delaunay_weights": (INT, [P, I64, P, I64, P, I64, P, P, P, P]),

@@ -96,6 +96,22 @@ def w_tilde_data_interferometer_from(visibilities_real, noise_map_real, uv_wavel
     return c.out(out)
 
 
+def dirty_image_from(visibilities, noise_map_real, uv_wavelengths, grid_radians_slim):
+    """Dirty image (M,) of complex visibilities (no reference function: the reference reads it from
+    its dataset): sum_k noise_k^-2 (Re V_k cos t - Im V_k sin t), t = 2 pi (x u_k + y v_k), with the
+    w_tilde pairing of grid and uv columns (numba.py:204)."""
+    c = Call("dirty_image_from")
+    v = c.complex_as_real(visibilities, "visibilities")
+    n = c.arr(noise_map_real, f64, 1, "noise_map_real")
+    uv = c.arr(uv_wavelengths, f64, 2, "uv_wavelengths")
+    g = c.arr(grid_radians_slim, f64, 2, "grid_radians_slim")
+    K, M = uv.shape[0], g.shape[0]
+    out = c.empty(M)
+    ws = c.workspace(_lib.load().aj_dirty_image_workspace_size(M, K))
+    _lib_call("aj_dirty_image", ptr(v), ptr(n), ptr(uv), ptr(g), K, M, ptr(out), ptr(ws), ws.numel(), c.stream())
+    return c.out(out)
+
+
 def w_tilde_curvature_interferometer_from(noise_map_real, uv_wavelengths, grid_radians_slim, *, precision="fp64",
                                           planes=False):
     """numba.py:156-207 — dense (M, M) w_tilde.

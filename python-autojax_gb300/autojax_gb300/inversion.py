@@ -244,8 +244,7 @@ class LogEvidence:
             raise np.linalg.LinAlgError(f"curvature_reg_matrix is not positive definite (pivot {where})")
         if code == _lib.AJ_INFO_INDEX_RANGE:
             raise IndexError(f"index out of range (flat position {where})")
-        if code == _lib.AJ_INFO_TIMEOUT:
-            raise RuntimeError(f"a bounded device wait ran out (block {where}); results are invalid")
+
 
     # --------------------------------------------------------- host facing
 
@@ -377,8 +376,7 @@ class LogEvidenceBatch:
                 raise np.linalg.LinAlgError(f"model {i}: curvature_reg_matrix is not positive definite (pivot {where})")
             if code == _lib.AJ_INFO_INDEX_RANGE:
                 raise IndexError(f"model {i}: index out of range (flat position {where})")
-            if code == _lib.AJ_INFO_TIMEOUT:
-                raise RuntimeError(f"model {i}: a bounded device wait ran out (block {where})")
+
 
 
 class LogEvidenceFunction(torch.autograd.Function):

@@ -38,13 +38,14 @@ int spd_inverse_from_factor(int64_t S, SpdWorkspace& w, double* Ainv, cudaStream
 // ---- lanes.cu (side streams that fork from and join back into the caller's stream)
 
 // 0: critical chain (highest priority), 1: bulk updates, 2: triangular inverse
-// (and A^-1) of the first matrix, 3: triangular inverse of the second
-constexpr int kLaneCount = 4;
+// of the first matrix, 3: triangular inverse of the second, 4: A^-1 of the first
+constexpr int kLaneCount = 5;
 enum LaneEvent {
     kEvFork = 0,
     kEvPanel,
     kEvUpdate,
     kEvDiag,
+    kEvRow,      // a block row of the first matrix's L^-1 is final
     kEvPre,      // the evaluation's independent pre-work forks here ...
     kEvPreDone,  // ... and is joined here
     kEvJoin0,
@@ -73,6 +74,7 @@ struct DfSpd {
     double* piv;     // the S pivots L_ii in float64
     double* vec;     // S scratch
     double* vec2;    // S scratch
+    float* part;     // partial sums of the transposed triangular product
 };
 size_t dfspd_bytes(int64_t S, bool with_inverse);
 DfSpd dfspd_carve(Carver& cv, int64_t S, bool with_inverse);
@@ -92,9 +94,8 @@ int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* 
 int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int count, int n_inverse, int64_t S,
                           DfSpd* const* w, double* const* logdet, int* info, cudaStream_t st, float* AIh = nullptr,
                           float* AIl = nullptr);
-// x = A^-1 b through A^-1's planes (full) when given, else through the inverse factor
-int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st, const float* AIh = nullptr,
-                    const float* AIl = nullptr);
+// x = A^-1 b through the inverse factor (two triangular products)
+int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st);
 int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x, double* r,
                         cudaStream_t st, const float* AIh = nullptr, const float* AIl = nullptr);
 int df_frob_lower(const float* h, const float* l, int64_t S, double* partial, int64_t nparts, cudaStream_t st);
@@ -126,7 +127,7 @@ int csc_spmm_t(const Csc& c, int64_t S, const Tin* X, int64_t ld_x, int64_t cols
                cudaStream_t st);
 // double-float planes: out (S x cols) = T^T X with X given as (hi, lo) planes
 int csc_spmm_t_df(const Csc& c, int64_t S, const float* Xh, const float* Xl, int64_t ld_x, int64_t cols, float* Oh,
-                  float* Ol, int64_t ld_out, int* info, cudaStream_t st);
+                  float* Ol, int64_t ld_out, cudaStream_t st);
 // out[s] = sum_e val[e] * x[row[e]]
 int csc_spmv_t(const Csc& c, int64_t S, const double* x, double* out, cudaStream_t st);
 // TW (S x M) with TW[s][m1] = sum_e val[e] * Wc(m1, row[e]) from the compact table (T float or double)

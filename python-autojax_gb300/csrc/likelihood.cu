@@ -524,11 +524,11 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
                 Wh = b.Wh;
                 Wl = b.Wl;
             }
-            AJ_TRY(csc_spmm_t_df(b.cs, S, Wh, Wl, M, M, b.TWh, b.TWl, M, info, st));
+            AJ_TRY(csc_spmm_t_df(b.cs, S, Wh, Wl, M, M, b.TWh, b.TWl, M, st));
         }
         AJ_TRY(transpose<float>(b.TWh, S, M, b.Omh, st));
         AJ_TRY(transpose<float>(b.TWl, S, M, b.Oml, st));
-        AJ_TRY(csc_spmm_t_df(b.cs, S, b.Omh, b.Oml, S, S, b.Fh, b.Fl, S, info, st));
+        AJ_TRY(csc_spmm_t_df(b.cs, S, b.Omh, b.Oml, S, S, b.Fh, b.Fl, S, st));
         AJ_TRY(join_pre());
         AJ_TRY(df_add_f64(b.Fh, b.Fl, b.H, S * S, b.Ah, b.Al, st));
         // A and H share every factorisation launch (and, with the gradient, every inversion launch)
@@ -560,12 +560,25 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         AJ_LAUNCHED();
     } else {
         AJ_TRY(df_split(b.s, S, b.sh, b.sl, st));
-        AJ_TRY(df_frob_lower(b.dh.Ih, b.dh.Il, S, b.fpart, b.nfrob, st));
     }
-    dlam_kernel<<<1, 1024, 0, st>>>(p->neighbors, p->neighbors_sizes, S, p->P, b.s, mixed ? nullptr : b.Ainv, b.AIh,
-                                    b.AIl, b.fpart, b.nfrob,
-                                    p->coefficient, p->coefficient_dev, mixed ? b.logdets + 4 : nullptr, out);
-    AJ_LAUNCHED();
+    // dlogE/dlambda (and, mixed, tr(H^-1)'s partial sums) on the side lane while st computes
+    // the weight gradient; both read only finished data
+    if (cudaEventRecord(ln.ev[kEvPre], st) != cudaSuccess || cudaStreamWaitEvent(pre, ln.ev[kEvPre], 0) != cudaSuccess)
+        return AJ_ERR_CUDA;
+    {
+        int rc = mixed ? df_frob_lower(b.dh.Ih, b.dh.Il, S, b.fpart, b.nfrob, pre) : AJ_OK;
+        if (rc == AJ_OK) {
+            dlam_kernel<<<1, 1024, 0, pre>>>(p->neighbors, p->neighbors_sizes, S, p->P, b.s, mixed ? nullptr : b.Ainv,
+                                             b.AIh, b.AIl, b.fpart, b.nfrob, p->coefficient, p->coefficient_dev,
+                                             mixed ? b.logdets + 4 : nullptr, out);
+            rc = check_launch();
+        }
+        if (cudaEventRecord(ln.ev[kEvPreDone], pre) != cudaSuccess) return AJ_ERR_CUDA;
+        if (rc != AJ_OK) {
+            cudaStreamWaitEvent(st, ln.ev[kEvPreDone], 0);
+            return rc;
+        }
+    }
     if (M > 0 && B > 0) {
         if (mixed)
             weight_grad_df_kernel<<<blocks_for(M * 32, 256), 256, 0, st>>>(
@@ -577,7 +590,7 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
                                                                         grad_weights);
         AJ_LAUNCHED();
     }
-    return AJ_OK;
+    return join_pre();
 }
 
 }  // extern "C"

@@ -769,6 +769,183 @@ __global__ void __launch_bounds__(128)
         }
 }
 
+// ------------------------------------------------- 64 x 64 tile updates
+//
+// The large steps of the trailing update, L^-1 and the streamed A^-1 use
+// 64 x 64 output tiles: 256 threads with 4 x 4 outputs each (rows ty + 16a,
+// columns tx + 16b) read k-major (hi, lo) pairs from shared memory, half a
+// shared load per double-float multiply-add against ~1.5 for the 32 x 32
+// kernels.  The order over k, the operand order and the renormalisation
+// points are those of the 32 x 32 kernels, so a step gives the same bits
+// whichever tile size runs it.
+constexpr int T64 = 64;
+
+struct Tile64 {
+    float2 a[DNB][T64 + 1];  // a[k][row of the output tile]
+    float2 b[DNB][T64 + 1];  // b[k][column of the output tile]
+};
+
+// acc[a][b] += sum_k A[k][ty + 16a] B[k][tx + 16b], lazy, renormalised every 8 k
+__device__ __forceinline__ void tile64_mac(const Tile64& t, df acc[4][4], int ty, int tx) {
+#pragma unroll
+    for (int k8 = 0; k8 < DNB; k8 += 8) {
+#pragma unroll 2
+        for (int k = k8; k < k8 + 8; ++k) {
+            float2 av[4], bv[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) av[i] = t.a[k][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) bv[j] = t.b[k][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) df_fma_lazy(acc[i][j], {av[i].x, av[i].y}, {bv[j].x, bv[j].y});
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) df_renorm(acc[i][j]);
+    }
+}
+
+// t.a[k][r] = M[(r0 + r) * S + c0 + k] for r < 64, k < 32 (rows r0.. of a 32-column block; zero outside S)
+__device__ __forceinline__ void load_rows_kmajor(float2 (*dst)[T64 + 1], const float* __restrict__ h,
+                                                 const float* __restrict__ l, int64_t S, int64_t r0, int64_t c0) {
+    for (int e = threadIdx.x; e < T64 * DNB; e += blockDim.x) {
+        const int r = e / DNB, k = e % DNB;
+        const bool in = r0 + r < S && c0 + k < S;
+        const int64_t off = (r0 + r) * S + c0 + k;
+        dst[k][r] = in ? make_float2(h[off], l[off]) : make_float2(0.f, 0.f);
+    }
+}
+
+// t.b[k][c] = M[(r0 + k) * S + c0 + c] for k < 32, c < 64 (32 rows, 64 columns; zero outside S)
+__device__ __forceinline__ void load_cols(float2 (*dst)[T64 + 1], const float* __restrict__ h,
+                                          const float* __restrict__ l, int64_t S, int64_t r0, int64_t c0) {
+    for (int e = threadIdx.x; e < T64 * DNB; e += blockDim.x) {
+        const int k = e / T64, c = e % T64;
+        const bool in = r0 + k < S && c0 + c < S;
+        const int64_t off = (r0 + k) * S + c0 + c;
+        dst[k][c] = in ? make_float2(h[off], l[off]) : make_float2(0.f, 0.f);
+    }
+}
+
+// Trailing update of step k0 past the next block column, 64 x 64 tiles from c1 = k0 + 64:
+// C -= P_i P_j^T (lower tiles; a diagonal tile writes its lower half)
+__global__ void __launch_bounds__(256)
+    dfsyrk_update64_kernel(DfMats mats, int64_t S, int64_t k0) {
+    float* __restrict__ Lh = pick(mats.Lh, blockIdx.y);
+    float* __restrict__ Ll = pick(mats.Ll, blockIdx.y);
+    __shared__ Tile64 t;
+    int64_t ti, tj;
+    lower_tile_df(blockIdx.x, ti, tj);
+    const int64_t c1 = k0 + 2 * DNB;
+    const int64_t i0 = c1 + ti * T64, j0 = c1 + tj * T64;
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    df cur[4][4], acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t gi = i0 + ty + 16 * i, gj = j0 + tx + 16 * j;
+            const bool in = gi < S && gj < S && gj <= gi;
+            cur[i][j] = in ? df{Lh[gi * S + gj], Ll[gi * S + gj]} : df{0.f, 0.f};
+            acc[i][j] = {0.f, 0.f};
+        }
+    load_rows_kmajor(t.a, Lh, Ll, S, i0, k0);
+    load_rows_kmajor(t.b, Lh, Ll, S, j0, k0);
+    __syncthreads();
+    tile64_mac(t, acc, ty, tx);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t gi = i0 + ty + 16 * i, gj = j0 + tx + 16 * j;
+            if (gi < S && gj < S && gj <= gi) {
+                const df v = df_add(cur[i][j], df_neg(acc[i][j]));
+                Lh[gi * S + gj] = v.hi;
+                Ll[gi * S + gj] = v.lo;
+            }
+        }
+}
+
+// L^-1 step kb for the rows past the next block row: X[i][j] += L[i][kb-block] X[kb-block][j]
+// over rows i >= (kb + 2) 32 and columns j < (kb + 1) 32, in 64 x 64 tiles (the next block row,
+// which also applies the diagonal inverse, stays with df_trtri_step_kernel)
+__global__ void __launch_bounds__(256)
+    df_trtri64_kernel(DfMats mats, int64_t S, int64_t kb) {
+    const float* __restrict__ Lh = pick(mats.Lh, blockIdx.y);
+    const float* __restrict__ Ll = pick(mats.Ll, blockIdx.y);
+    float* __restrict__ Ih = pick(mats.Ih, blockIdx.y);
+    float* __restrict__ Il = pick(mats.Il, blockIdx.y);
+    __shared__ Tile64 t;
+    const int64_t ncol = (kb + 1) * DNB;  // columns of X that are nonzero in block row kb
+    const int64_t nJ = (ncol + T64 - 1) / T64;
+    const int64_t I = blockIdx.x / nJ, J = blockIdx.x % nJ;
+    const int64_t i0 = (kb + 2) * DNB + I * T64, j0 = J * T64, p0 = kb * DNB;
+    if (i0 >= S) return;
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    df acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t gi = i0 + ty + 16 * i, gj = j0 + tx + 16 * j;
+            const bool in = gi < S && gj < ncol;
+            acc[i][j] = in ? df{Ih[gi * S + gj], Il[gi * S + gj]} : df{0.f, 0.f};
+        }
+    load_rows_kmajor(t.a, Lh, Ll, S, i0, p0);
+    load_cols(t.b, Ih, Il, S, p0, j0);
+    __syncthreads();
+    tile64_mac(t, acc, ty, tx);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t gi = i0 + ty + 16 * i, gj = j0 + tx + 16 * j;
+            if (gi < S && gj < ncol) {
+                Ih[gi * S + gj] = acc[i][j].hi;
+                Il[gi * S + gj] = acc[i][j].lo;
+            }
+        }
+}
+
+// Streamed A^-1 for block row R of X = L^-1 in 64 x 64 tiles (I, J), J <= I, over the first
+// (R + 1) 32 rows and columns: C[i][j] += sum_c X[R 32 + c][i] X[R 32 + c][j]
+__global__ void __launch_bounds__(256)
+    df_lauum64_kernel(const float* __restrict__ Xh, const float* __restrict__ Xl, float* __restrict__ Ch,
+                      float* __restrict__ Cl, int64_t S, int64_t R) {
+    __shared__ Tile64 t;
+    int64_t ti, tj;
+    lower_tile_df(blockIdx.x, ti, tj);
+    const int64_t lim = (R + 1) * DNB < S ? (R + 1) * DNB : S;  // X row block R is zero past column lim
+    const int64_t i0 = ti * T64, j0 = tj * T64, r0 = R * DNB;
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    df cur[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t gi = i0 + ty + 16 * i, gj = j0 + tx + 16 * j;
+            const bool in = gi < lim && gj < lim;
+            cur[i][j] = in ? df{Ch[gi * S + gj], Cl[gi * S + gj]} : df{0.f, 0.f};
+        }
+    load_cols(t.a, Xh, Xl, S, r0, i0);
+    load_cols(t.b, Xh, Xl, S, r0, j0);
+    __syncthreads();
+    tile64_mac(t, cur, ty, tx);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t gi = i0 + ty + 16 * i, gj = j0 + tx + 16 * j;
+            if (gi < lim && gj < lim) {
+                Ch[gi * S + gj] = cur[i][j].hi;
+                Cl[gi * S + gj] = cur[i][j].lo;
+            }
+        }
+}
+
 __global__ void df_mirror_lower_kernel(float* __restrict__ h, float* __restrict__ l, int64_t S) {
     for (int64_t i = blockIdx.y; i < S; i += gridDim.y)
         for (int64_t j = i + 1 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < S;
@@ -810,24 +987,47 @@ __global__ void __launch_bounds__(256)
     if (lane == 0) store_y(v, i, y, yh, yl);
 }
 
-// y = Li^T x: y[i] = sum_{j >= i} Li[j][i] x[j]; one warp per output, lanes
-// over the rows j (column access: the path without A^-1 uses it twice per solve)
+// y = Li^T x: y[i] = sum_{j >= i} Li[j][i] x[j], in two passes.  Pass 1: block
+// (i-group of 32 columns, j-chunk of TRMV_ROWS rows) reads its tile row by row
+// (one coalesced 128-byte line per row and plane), its 8 warps split the rows
+// and meet in shared memory; the chunk's partial sums go to part[chunk][i].
+// Pass 2 adds the chunks in order, so the result does not depend on timing.
+constexpr int TRMV_ROWS = 64;
+
 __global__ void __launch_bounds__(256)
-    df_trmv_t_kernel(const float* __restrict__ Lh, const float* __restrict__ Ll, int64_t S,
-                     const float* __restrict__ xh, const float* __restrict__ xl, double* __restrict__ y,
-                     float* __restrict__ yh, float* __restrict__ yl) {
-    const int lane = threadIdx.x & 31;
-    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (i >= S) return;
-    df acc[2] = {{0.f, 0.f}, {0.f, 0.f}};
-    int64_t j = i + lane;
-    for (; j + 32 < S; j += 64) {
-        df_fma_acc(acc[0], {Lh[j * S + i], Ll[j * S + i]}, {xh[j], xl[j]});
-        df_fma_acc(acc[1], {Lh[(j + 32) * S + i], Ll[(j + 32) * S + i]}, {xh[j + 32], xl[j + 32]});
+    df_trmv_t_part_kernel(const float* __restrict__ Lh, const float* __restrict__ Ll, int64_t S,
+                          const float* __restrict__ xh, const float* __restrict__ xl, float* __restrict__ ph,
+                          float* __restrict__ pl) {
+    __shared__ float sh[8][32], sl[8][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t i0 = (int64_t)blockIdx.x * 32, i = i0 + lane;
+    const int64_t j0 = (int64_t)blockIdx.y * TRMV_ROWS;
+    df acc = {0.f, 0.f};
+    if (j0 + TRMV_ROWS > i0) {  // otherwise the whole tile is above the diagonal
+        for (int r = warp; r < TRMV_ROWS; r += 8) {
+            const int64_t j = j0 + r;
+            if (j < S && i < S && j >= i) df_fma_acc(acc, {Lh[j * S + i], Ll[j * S + i]}, {xh[j], xl[j]});
+        }
     }
-    for (; j < S; j += 32) df_fma_acc(acc[0], {Lh[j * S + i], Ll[j * S + i]}, {xh[j], xl[j]});
-    const double v = warp_sum(df_to(df_add(acc[0], acc[1])));
-    if (lane == 0) store_y(v, i, y, yh, yl);
+    sh[warp][lane] = acc.hi;
+    sl[warp][lane] = acc.lo;
+    __syncthreads();
+    if (warp == 0 && i < S) {
+        df tot = {sh[0][lane], sl[0][lane]};
+        for (int w = 1; w < 8; ++w) tot = df_add(tot, {sh[w][lane], sl[w][lane]});
+        ph[blockIdx.y * S + i] = tot.hi;
+        pl[blockIdx.y * S + i] = tot.lo;
+    }
+}
+
+__global__ void df_trmv_t_sum_kernel(const float* __restrict__ ph, const float* __restrict__ pl, int64_t S,
+                                     int64_t nchunk, double* __restrict__ y, float* __restrict__ yh,
+                                     float* __restrict__ yl) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < S; i += (int64_t)gridDim.x * blockDim.x) {
+        df tot = {0.f, 0.f};
+        for (int64_t c = i / TRMV_ROWS; c < nchunk; ++c) tot = df_add(tot, {ph[c * S + i], pl[c * S + i]});
+        store_y(df_to(tot), i, y, yh, yl);
+    }
 }
 
 // y = A x, or y = b - A x when b is set, for a full double-float A (x as
@@ -883,6 +1083,7 @@ size_t dfspd_bytes(int64_t S, bool with_inverse) {
     s.take<double>(S);  // pivots
     s.take<double>(S);  // vector scratch
     s.take<double>(S);  // vector scratch
+    s.take<float>(2 * ((S + TRMV_ROWS - 1) / TRMV_ROWS) * S);  // transposed-product partial sums
     return s.total();
 }
 
@@ -908,6 +1109,7 @@ DfSpd dfspd_carve(Carver& cv, int64_t S, bool with_inverse) {
     w.piv = cv.take<double>(S);
     w.vec = cv.take<double>(S);
     w.vec2 = cv.take<double>(S);
+    w.part = cv.take<float>(2 * ((S + TRMV_ROWS - 1) / TRMV_ROWS) * S);
     return w;
 }
 
@@ -949,6 +1151,11 @@ static DfMats mats_of(DfSpd* const* w, int count) {
     return m;
 }
 
+// When a step switches from 32 x 32 to 64 x 64 tiles: the minimum number of
+// 64 x 64 output tiles per matrix (below it the 32 x 32 kernels, with 4x the
+// blocks, fill the GPU better).  Set by aj_set_tile_policy (the autotuner).
+static int g_tile64_min[3] = {128, 128, 96};  // trailing update, L^-1 step, A^-1 row
+
 // L (in w[z]) = chol(A[z]) for z < count (1 or 2), and L^-1 for z < n_inverse; A given as planes
 // (copied unless it is w's own L).
 //
@@ -988,9 +1195,9 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
     Lanes* lanes = nullptr;
     AJ_TRY(lanes_for(st, &lanes));
     Lanes& ln = *lanes;
-    const int nlanes = 2 + n_inverse;
+    const int nlanes = AIh ? 5 : 2 + n_inverse;  // lanes 2 .. 1 + n_inverse for L^-1, lane 4 for A^-1
     AJ_TRY(lanes_fork(ln, st, nlanes));
-    cudaStream_t crit = ln.s[0], bulk = ln.s[1], tri = ln.s[2];
+    cudaStream_t crit = ln.s[0], bulk = ln.s[1];
     // each matrix's L^-1 on its own lane: a view of m whose slot 0 is matrix z
     DfMats one[2] = {m, m};
     for (int z = 0; z < 2; ++z) {
@@ -1022,13 +1229,20 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
     };
     // A^-1 of matrix 0, one final block row of its L^-1 at a time
     auto lauum_row = [&](int64_t R, cudaStream_t on) {
-        const int64_t tiles = (R + 1) * (R + 2) / 2;
-        df_lauum_row_kernel<<<(unsigned)tiles, 128, 0, on>>>(w[0]->Ih, w[0]->Il, AIh, AIl, S, R);
+        const int64_t lim = (R + 1) * DNB < S ? (R + 1) * DNB : S;
+        const int64_t nT = (lim + T64 - 1) / T64;
+        if (nT * (nT + 1) / 2 >= g_tile64_min[2]) {
+            df_lauum64_kernel<<<(unsigned)(nT * (nT + 1) / 2), 256, 0, on>>>(w[0]->Ih, w[0]->Il, AIh, AIl, S, R);
+        } else {
+            const int64_t tiles = (R + 1) * (R + 2) / 2;
+            df_lauum_row_kernel<<<(unsigned)tiles, 128, 0, on>>>(w[0]->Ih, w[0]->Il, AIh, AIl, S, R);
+        }
         return check_launch();
     };
     // Step kb: panel kb + 1 applies panel kb's update to its own block column,
     // so it only has to wait for the bulk update of step kb - 1 (which reached
     // that column); the bulk update of step kb covers the columns after it.
+    cudaStream_t lau = ln.s[4];
     AJ_TRY(panel(0));
     if (AIh && nbt == 1) AJ_TRY(lauum_row(0, crit));
     bool rest_prev = false;
@@ -1040,7 +1254,12 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
         if (tb > 1) {
             AJ_TRY(lane_signal(ln, kEvPanel, 0));
             AJ_TRY(lane_wait(ln, 1, kEvPanel));
-            dfsyrk_update_kernel<<<dim3((unsigned)((tb - 1) * tb / 2), count), 128, 0, bulk>>>(m, S, k0);
+            const int64_t n64 = (S - k0 - 2 * DNB + T64 - 1) / T64;
+            const int64_t t64 = n64 * (n64 + 1) / 2;
+            if (t64 >= g_tile64_min[0])
+                dfsyrk_update64_kernel<<<dim3((unsigned)t64, count), 256, 0, bulk>>>(m, S, k0);
+            else
+                dfsyrk_update_kernel<<<dim3((unsigned)((tb - 1) * tb / 2), count), 128, 0, bulk>>>(m, S, k0);
             AJ_LAUNCHED();
             AJ_TRY(lane_signal(ln, kEvUpdate, 1));
         }
@@ -1048,15 +1267,27 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
         AJ_TRY(panel(kb + 1));
         if (n_inverse > 0) {
             AJ_TRY(lane_signal(ln, kEvDiag, 0));
-            const int64_t tiles = (nbt - kb - 1) * (kb + 1);
+            // rows past the next block row in 64 x 64 tiles when there are enough of them; the
+            // next block row (which applies the diagonal inverse) always in 32 x 32 tiles
+            const int64_t nI = (S - (kb + 2) * DNB + T64 - 1) / T64, nJ = ((kb + 1) * DNB + T64 - 1) / T64;
+            const bool big = nI > 0 && nI * nJ >= g_tile64_min[1];
+            const int64_t tiles = (big ? 1 : nbt - kb - 1) * (kb + 1);
             for (int z = 0; z < n_inverse; ++z) {
                 AJ_TRY(lane_wait(ln, 2 + z, kEvDiag));
                 df_trtri_step_kernel<<<(unsigned)tiles, 256, 0, ln.s[2 + z]>>>(one[z], S, kb);
                 AJ_LAUNCHED();
+                if (big) {
+                    df_trtri64_kernel<<<(unsigned)(nI * nJ), 256, 0, ln.s[2 + z]>>>(one[z], S, kb);
+                    AJ_LAUNCHED();
+                }
             }
             // block row 0 of L^-1 is final since panel 0, block row kb + 1 after this step
-            if (AIh && kb == 0) AJ_TRY(lauum_row(0, tri));
-            if (AIh) AJ_TRY(lauum_row(kb + 1, tri));
+            if (AIh) {
+                AJ_TRY(lane_signal(ln, kEvRow, 2));
+                AJ_TRY(lane_wait(ln, 4, kEvRow));
+                if (kb == 0) AJ_TRY(lauum_row(0, lau));
+                AJ_TRY(lauum_row(kb + 1, lau));
+            }
         }
     }
     df_store_diag_kernel<<<dim3((unsigned)nbt, count), 256, 0, crit>>>(m, S);
@@ -1076,36 +1307,48 @@ int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* 
     return dfspd_factor_invert_n(&Ah, &Al, 1, 0, S, ws, ld, info, st, nullptr, nullptr);
 }
 
-// x = A^-1 b, b and x may alias.  With A^-1's planes (AIh/AIl, full) it is one
-// row-wise product; otherwise Li^T (Li b) with the inverse factor.  The
+// x = A^-1 b = Li^T (Li b) with the inverse factor, b and x may alias.  The
 // scratch vectors hold b's and Li b's planes (S hi floats, then S lo floats).
-int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st, const float* AIh,
-                    const float* AIl) {
+// (Two triangular products split the conditioning between two factors of
+// sqrt(cond A); one product with an explicit A^-1 would lose cond(A) at once.)
+int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st) {
+    if (!w.Ih) return AJ_ERR_ARG;
     float* bh = reinterpret_cast<float*>(w.vec);
+    float* uh = reinterpret_cast<float*>(w.vec2);
     AJ_TRY(df_split(b, S, bh, bh + S, st));
     const unsigned g = blocks_for(S * 32, 256);
-    if (AIh) {
-        df_gemv_kernel<<<g, 256, 0, st>>>(AIh, AIl, S, bh, bh + S, nullptr, x, nullptr, nullptr);
-        return check_launch();
-    }
-    if (!w.Ih) return AJ_ERR_ARG;
-    float* uh = reinterpret_cast<float*>(w.vec2);
     df_trmv_kernel<<<g, 256, 0, st>>>(w.Ih, w.Il, S, bh, bh + S, nullptr, uh, uh + S);
     AJ_LAUNCHED();
-    df_trmv_t_kernel<<<g, 256, 0, st>>>(w.Ih, w.Il, S, uh, uh + S, x, nullptr, nullptr);
+    const int64_t nchunk = (S + TRMV_ROWS - 1) / TRMV_ROWS;
+    float* ph = w.part;
+    float* pl = w.part + nchunk * S;
+    df_trmv_t_part_kernel<<<dim3((unsigned)((S + 31) / 32), (unsigned)nchunk), 256, 0, st>>>(w.Ih, w.Il, S, uh,
+                                                                                           uh + S, ph, pl);
+    AJ_LAUNCHED();
+    df_trmv_t_sum_kernel<<<blocks_for(S, 256, 64), 256, 0, st>>>(ph, pl, S, nchunk, x, nullptr, nullptr);
     return check_launch();
 }
 
-// x = A^-1 b with one step of iterative refinement against A (planes); r is S scratch
+// x = A^-1 b with one step of iterative refinement against A (planes); r is S
+// scratch.  The correction A^-1 r goes through A^-1's planes (one row-wise
+// product) when they are given: r is already small, so the explicit inverse's
+// cond(A) loss applies to a correction, not to the solution.
 int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x, double* r,
                         cudaStream_t st, const float* AIh, const float* AIl) {
-    AJ_TRY(dfspd_solve_vec(S, w, b, x, st, AIh, AIl));
+    AJ_TRY(dfspd_solve_vec(S, w, b, x, st));
     const unsigned g = blocks_for(S * 32, 256);
     float* xh = reinterpret_cast<float*>(w.vec);
     AJ_TRY(df_split(x, S, xh, xh + S, st));
     df_gemv_kernel<<<g, 256, 0, st>>>(Ah, Al, S, xh, xh + S, b, r, nullptr, nullptr);
     AJ_LAUNCHED();
-    AJ_TRY(dfspd_solve_vec(S, w, r, r, st, AIh, AIl));
+    if (AIh) {
+        float* rh = reinterpret_cast<float*>(w.vec2);
+        AJ_TRY(df_split(r, S, rh, rh + S, st));
+        df_gemv_kernel<<<g, 256, 0, st>>>(AIh, AIl, S, rh, rh + S, nullptr, r, nullptr, nullptr);
+        AJ_LAUNCHED();
+    } else {
+        AJ_TRY(dfspd_solve_vec(S, w, r, r, st));
+    }
     add_vec_kernel<<<blocks_for(S, 256, 64), 256, 0, st>>>(x, r, S);
     return check_launch();
 }
@@ -1120,6 +1363,20 @@ int df_frob_lower(const float* h, const float* l, int64_t S, double* partial, in
 using namespace aj;
 
 extern "C" {
+
+int aj_set_tile_policy(int update_min_tiles, int inverse_min_tiles, int lauum_min_tiles) {
+    if (update_min_tiles < 1 || inverse_min_tiles < 1 || lauum_min_tiles < 1) return AJ_ERR_ARG;
+    aj::g_tile64_min[0] = update_min_tiles;
+    aj::g_tile64_min[1] = inverse_min_tiles;
+    aj::g_tile64_min[2] = lauum_min_tiles;
+    return AJ_OK;
+}
+
+int aj_get_tile_policy(int* out3) {
+    if (!out3) return AJ_ERR_ARG;
+    for (int i = 0; i < 3; ++i) out3[i] = aj::g_tile64_min[i];
+    return AJ_OK;
+}
 
 size_t aj_spd_inverse_mixed_workspace_size(int64_t S) {
     Sizer s;

@@ -271,142 +271,71 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// TMA variant of the double-float gather.  A block owns one source pixel s
-// and a chunk of GATHER_CW columns; entry k of s needs the chunk of row
-// rows[q] of both planes (GATHER_CW floats each).  One thread streams those
-// row chunks into GATHER_STAGES shared-memory stages with bulk async copies
-// (cp.async.bulk, completion on an mbarrier per stage), GATHER_STAGES entries
-// ahead of the consumers, so the memory pipeline stays full without registers
-// or per-thread address arithmetic; every thread then only reads its 4
-// columns from shared memory and accumulates.  Waits are bounded: a stage that
-// never completes sets AJ_INFO_TIMEOUT in info and the block stops after its
-// copies in flight have landed (also a bounded wait).
-constexpr int GATHER_CW = 1024;
-constexpr int GATHER_STAGES = 6;
-constexpr size_t GATHER_SMEM = sizeof(float) * 2 * GATHER_CW * GATHER_STAGES + 8 * GATHER_STAGES;
-constexpr long long GATHER_SPIN_LIMIT = 1ll << 24;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
-    unsigned done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return done != 0;
-}
-
-// bounded wait for the phase with the given parity; false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
-    for (long long i = 0; i < GATHER_SPIN_LIMIT; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(dst)),
-        "l"(src), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
+// The float4 fast path of the double-float gather (X rows 16-byte aligned,
+// cols % 4 == 0).  It is latency-bound, so entries go four at a time with the
+// next group's rows loaded while the current group accumulates.  A group
+// running past the column's end reads row rows[b] with weight 0, which adds
+// exactly nothing.  Accumulation is lazy, renormalised every 8 entries.
+__device__ __forceinline__ void gather_group(const int* __restrict__ rows, const float2* __restrict__ vdf,
+                                             const float* __restrict__ Xh, const float* __restrict__ Xl,
+                                             int64_t ld_x, int64_t c0, int q, int b, int e, float4* h, float4* l,
+                                             float2* a) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const bool in = q + u < e;
+        const int qq = in ? q + u : b;
+        const int64_t off = (int64_t)rows[qq] * ld_x + c0;
+        h[u] = __ldg(reinterpret_cast<const float4*>(Xh + off));
+        l[u] = __ldg(reinterpret_cast<const float4*>(Xl + off));
+        a[u] = in ? vdf[qq] : make_float2(0.f, 0.f);
+    }
 }
 
 __global__ void __launch_bounds__(256)
-    csc_spmm_t_df_tma_kernel(const int* __restrict__ colptr, const int* __restrict__ rows,
+    csc_spmm_t_df_vec_kernel(const int* __restrict__ colptr, const int* __restrict__ rows,
                              const float2* __restrict__ vdf, const float* __restrict__ Xh,
                              const float* __restrict__ Xl, int64_t ld_x, int64_t cols, float* __restrict__ Oh,
-                             float* __restrict__ Ol, int64_t ld_out, int* info) {
-    extern __shared__ __align__(128) unsigned char gather_smem[];
-    float* stage = reinterpret_cast<float*>(gather_smem);  // [stage][hi GATHER_CW | lo GATHER_CW]
-    uint64_t* bar = reinterpret_cast<uint64_t*>(gather_smem + sizeof(float) * 2 * GATHER_CW * GATHER_STAGES);
+                             float* __restrict__ Ol, int64_t ld_out) {
     const int64_t s = blockIdx.x;
-    const int64_t cbase = (int64_t)blockIdx.y * GATHER_CW;
-    const int64_t cw = (cols - cbase) < GATHER_CW ? (cols - cbase) : GATHER_CW;  // multiple of 4
-    const unsigned bytes = (unsigned)(cw * sizeof(float));
-    const int tid = threadIdx.x;
+    const int64_t c0 = (blockIdx.y * (int64_t)blockDim.x + threadIdx.x) * 4;
+    if (c0 >= cols) return;
     const int b = colptr[s], e = colptr[s + 1];
-    const int n = e - b;
-    __shared__ int failed;
-    if (tid == 0) {
-        for (int k = 0; k < GATHER_STAGES; ++k) mbar_init(&bar[k], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        failed = 0;
-    }
-    __syncthreads();
-    auto issue = [&](int k) {  // thread 0: entry k into stage k % GATHER_STAGES
-        const int st = k % GATHER_STAGES;
-        const int64_t off = (int64_t)rows[b + k] * ld_x + cbase;
-        float* dst = stage + (int64_t)st * 2 * GATHER_CW;
-        mbar_expect_tx(&bar[st], 2 * bytes);
-        bulk_g2s(dst, Xh + off, bytes, &bar[st]);
-        bulk_g2s(dst + GATHER_CW, Xl + off, bytes, &bar[st]);
-    };
-    int issued = 0;  // thread 0's count of entries handed to the copy engine
-    if (tid == 0) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        for (; issued < n && issued < GATHER_STAGES; ++issued) issue(issued);
-    }
-    const int c = tid * 4;  // this thread's 4 columns within the chunk
     df acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    int consumed = 0;
-    for (int k = 0; k < n; ++k, ++consumed) {
-        const int st = k % GATHER_STAGES;
-        const unsigned parity = (unsigned)((k / GATHER_STAGES) & 1);
-        if (!mbar_wait(&bar[st], parity)) failed = 1;
-        __syncthreads();
-        if (failed) break;
-        if (c < cw) {
-            const float* sh = stage + (int64_t)st * 2 * GATHER_CW;
-            const float4 h = *reinterpret_cast<const float4*>(sh + c);
-            const float4 l = *reinterpret_cast<const float4*>(sh + GATHER_CW + c);
-            const float2 wv = vdf[b + k];
-            const df w = {wv.x, wv.y};
-            df_fma_lazy(acc[0], w, {h.x, l.x});
-            df_fma_lazy(acc[1], w, {h.y, l.y});
-            df_fma_lazy(acc[2], w, {h.z, l.z});
-            df_fma_lazy(acc[3], w, {h.w, l.w});
-            if ((k & 7) == 7)
+    if (b < e) {
+        float4 h[4], l[4];
+        float2 a[4];
+        gather_group(rows, vdf, Xh, Xl, ld_x, c0, b, b, e, h, l, a);
+        int group = 0;
+        for (int q = b; q < e; q += 4) {
+            float4 hn[4], ln[4];
+            float2 an[4];
+            const bool more = q + 4 < e;
+            if (more) gather_group(rows, vdf, Xh, Xl, ld_x, c0, q + 4, b, e, hn, ln, an);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const df w = {a[u].x, a[u].y};
+                df_fma_lazy(acc[0], w, {h[u].x, l[u].x});
+                df_fma_lazy(acc[1], w, {h[u].y, l[u].y});
+                df_fma_lazy(acc[2], w, {h[u].z, l[u].z});
+                df_fma_lazy(acc[3], w, {h[u].w, l[u].w});
+            }
+            if (++group % 2 == 0)
 #pragma unroll
                 for (int v = 0; v < 4; ++v) df_renorm(acc[v]);
+            if (more) {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    h[u] = hn[u];
+                    l[u] = ln[u];
+                    a[u] = an[u];
+                }
+            }
         }
-        __syncthreads();  // every thread is done with stage st before it is refilled
-        if (tid == 0 && issued < n) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(issued++);
-        }
-    }
-    if (failed) {
-        // the copies still in flight (entries consumed .. issued - 1) land before the block's
-        // shared memory is released; these waits are bounded too
-        if (tid == 0) {
-            report(info, AJ_INFO_TIMEOUT, s);
-            for (int k = consumed; k < issued; ++k)
-                (void)mbar_wait(&bar[k % GATHER_STAGES], (unsigned)((k / GATHER_STAGES) & 1));
-        }
-        __syncthreads();
-        return;
-    }
-    if (c < cw) {
 #pragma unroll
         for (int v = 0; v < 4; ++v) df_renorm(acc[v]);
-        *reinterpret_cast<float4*>(Oh + s * ld_out + cbase + c) = make_float4(acc[0].hi, acc[1].hi, acc[2].hi, acc[3].hi);
-        *reinterpret_cast<float4*>(Ol + s * ld_out + cbase + c) = make_float4(acc[0].lo, acc[1].lo, acc[2].lo, acc[3].lo);
     }
+    *reinterpret_cast<float4*>(Oh + s * ld_out + c0) = make_float4(acc[0].hi, acc[1].hi, acc[2].hi, acc[3].hi);
+    *reinterpret_cast<float4*>(Ol + s * ld_out + c0) = make_float4(acc[0].lo, acc[1].lo, acc[2].lo, acc[3].lo);
 }
 
 __global__ void csc_spmv_t_kernel(const int* __restrict__ colptr, const int* __restrict__ rows,
@@ -594,26 +523,15 @@ template int csc_spmm_t<float, double>(const Csc&, int64_t, const float*, int64_
                                        cudaStream_t);
 
 int csc_spmm_t_df(const Csc& c, int64_t S, const float* Xh, const float* Xl, int64_t ld_x, int64_t cols, float* Oh,
-                  float* Ol, int64_t ld_out, int* info, cudaStream_t st) {
+                  float* Ol, int64_t ld_out, cudaStream_t st) {
     if (S == 0 || cols == 0) return AJ_OK;
     dim3 grid((unsigned)S, (unsigned)((cols / 4 + 1 + 255) / 256));
     const bool vec = (cols % 4 == 0) && (ld_x % 4 == 0) && (ld_out % 4 == 0) &&
                      (reinterpret_cast<uintptr_t>(Xh) % 16 == 0) && (reinterpret_cast<uintptr_t>(Xl) % 16 == 0) &&
                      (reinterpret_cast<uintptr_t>(Oh) % 16 == 0) && (reinterpret_cast<uintptr_t>(Ol) % 16 == 0);
-    if (vec) {
-        static bool attr_set[64] = {};
-        int dev = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess) return AJ_ERR_CUDA;
-        if (dev < 64 && !attr_set[dev]) {
-            if (cudaFuncSetAttribute(csc_spmm_t_df_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)GATHER_SMEM) != cudaSuccess)
-                return AJ_ERR_CUDA;
-            attr_set[dev] = true;
-        }
-        const dim3 tgrid((unsigned)S, (unsigned)((cols + GATHER_CW - 1) / GATHER_CW));
-        csc_spmm_t_df_tma_kernel<<<tgrid, 256, GATHER_SMEM, st>>>(c.colptr, c.rows, c.vdf, Xh, Xl, ld_x, cols, Oh, Ol,
-                                                                  ld_out, info);
-    } else
+    if (vec)
+        csc_spmm_t_df_vec_kernel<<<grid, 256, 0, st>>>(c.colptr, c.rows, c.vdf, Xh, Xl, ld_x, cols, Oh, Ol, ld_out);
+    else
         csc_spmm_t_df_kernel<<<grid, 256, 0, st>>>(c.colptr, c.rows, c.vdf, Xh, Xl, ld_x, cols, Oh, Ol, ld_out);
     return check_launch();
 }

@@ -293,13 +293,15 @@ __global__ void compact_assemble_kernel(const double* __restrict__ accum, int64_
 // --------------------------------------------------------------- cos sums
 
 // partial[split][c] = sum over this split's k of a_k cos(2 pi (X_c u_k + Y_c v_k)).
-// Weight modes: 0 -> a_k = sigma_k^-2 (w_tilde), 1 -> a_k = (sigma_k^2 / vis_k)^2 (w_tilde_data).
+// Weight modes: 0 -> a_k = sigma_k^-2 (w_tilde), 1 -> a_k = (sigma_k^2 / vis_k)^2 (w_tilde_data),
+// 2 -> the dirty image (float64 only): a_k cos + b_k sin with a_k = sigma_k^-2 Re V_k,
+// b_k = -sigma_k^-2 Im V_k, vis interleaved complex.
 template <bool MIXED>
 __global__ void __launch_bounds__(256)
     cos_sum_kernel(const double* __restrict__ X, const double* __restrict__ Y, int64_t stride, int64_t C,
                    const double* __restrict__ uv, const double* __restrict__ sigma, const double* __restrict__ vis,
                    int weight_mode, int64_t K, int64_t k_per_split, double* __restrict__ partial) {
-    __shared__ double su[512], sv[512], sa[512];
+    __shared__ double su[512], sv[512], sa[512], sb[512];
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const double x = c < C ? X[c * stride] : 0.0;
     const double y = c < C ? Y[c * stride] : 0.0;
@@ -317,6 +319,10 @@ __global__ void __launch_bounds__(256)
             const double s = sigma[k];
             if (weight_mode == 0) {
                 sa[e] = 1.0 / (s * s);
+            } else if (weight_mode == 2) {
+                const double w = 1.0 / (s * s);
+                sa[e] = w * vis[2 * k];
+                sb[e] = -w * vis[2 * k + 1];
             } else {
                 const double q = (s * s) / vis[k];
                 sa[e] = q * q;
@@ -334,6 +340,10 @@ __global__ void __launch_bounds__(256)
                         accf = 0.f;
                         cnt = 0;
                     }
+                } else if (weight_mode == 2) {
+                    double sn, cs;
+                    sincospi(2.0 * t, &sn, &cs);
+                    acc = fma(sa[e], cs, fma(sb[e], sn, acc));
                 } else {
                     acc = fma(sa[e], cospi(2.0 * t), acc);
                 }
@@ -698,6 +708,28 @@ int aj_w_tilde_data(const double* visibilities_real, const double* noise_map_rea
     // numba.py:151: cos(g_2pi[i,1] u_k0 + g_2pi[i,0] u_k1): X = grid[:, 1], Y = grid[:, 0]
     return launch_cos_sum(grid_slim + 1, grid_slim, 2, M, uv, noise_map_real, visibilities_real, 1, K, nullptr, out,
                           partial, pl, precision, st);
+}
+
+size_t aj_dirty_image_workspace_size(int64_t M, int64_t K) {
+    CosSumPlan pl = cos_sum_plan(M, K);
+    Sizer s;
+    s.take<double>(pl.nsplit * M);
+    return s.total();
+}
+
+int aj_dirty_image(const double* visibilities, const double* noise_map_real, const double* uv,
+                   const double* grid_slim, int64_t K, int64_t M, double* out, void* workspace,
+                   size_t workspace_bytes, void* stream) {
+    if (M < 0 || K < 0) return AJ_ERR_ARG;
+    if (M == 0) return AJ_OK;
+    if (!out || !grid_slim || (K > 0 && (!noise_map_real || !uv || !visibilities))) return AJ_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    if (K == 0) return cudaMemsetAsync(out, 0, sizeof(double) * M, st) == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+    CosSumPlan pl = cos_sum_plan(M, K);
+    if (!workspace || workspace_bytes < aj_dirty_image_workspace_size(M, K)) return AJ_ERR_WORKSPACE;
+    // phase 2 pi (x u + y v) with x = grid[:, 1], y = grid[:, 0], the w_tilde pairing (numba.py:204)
+    return launch_cos_sum(grid_slim + 1, grid_slim, 2, M, uv, noise_map_real, visibilities, 2, K, nullptr, out,
+                          static_cast<double*>(workspace), pl, AJ_FP64, st);
 }
 
 int aj_w_tilde_via_compact(const double* w_compact, int64_t N, const int64_t* native_index, int64_t M,

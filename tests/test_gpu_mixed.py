@@ -174,3 +174,63 @@ def test_mixed_spd_inverse_reports_not_positive_definite():
     torch.cuda.synchronize()
     assert int(info[0]) == _lib.AJ_INFO_NOT_POSITIVE_DEFINITE
     assert np.isnan(float(logdet[0]))
+
+
+@pytest.mark.parametrize("config,K", [("cfg2", 3000)])
+def test_mixed_matches_fp64_at_multi_chunk_sizes(aj, config, K):
+    """M = 5,024 > 1,024: the double-float gathers run over several column chunks (the golden cases
+    have M <= 1,024).  Mixed logE against the float64 path (itself pinned to the oracle) over the
+    bench's lambda range."""
+    import torch
+
+    from autojax_gb300 import synthetic
+    from autojax_gb300.inversion import Dataset, LogEvidence
+
+    d = synthetic.make_dataset(config, K=K)
+    dev = torch.device("cuda")
+    wc = aj.w_compact_curvature_interferometer_from(d["grid_size"], torch.from_numpy(d["noise_map_real"]).to(dev),
+                                                    torch.from_numpy(d["uv_wavelengths"]).to(dev), d["pixel_scale"])
+    W = aj.w_tilde_via_compact_from(wc, torch.from_numpy(d["native_index_for_slim_index"]).to(dev))
+    B, P = d["pix_indexes_for_sub_slim_index"].shape[1], d["neighbors"].shape[1]
+    ev = {p: LogEvidence(S=d["S"], B=B, P=P, precision=p,
+                         dataset=Dataset(d["dirty_image"], d["data"], d["noise_map"], W, precision=p))
+          for p in ("mixed", "fp64")}
+    for lam in (1e-3, 1e-1, 1e1, 1e3):
+        out = {}
+        for p, e in ev.items():
+            e.set_model(d["pix_indexes_for_sub_slim_index"], d["pix_weights_for_sub_slim_index"], d["neighbors"],
+                        d["neighbors_sizes"], np.sqrt(lam))
+            e.launch()
+            torch.cuda.synchronize()
+            e.check()
+            out[p] = e.out.cpu().numpy().copy()
+        assert abs(out["mixed"][0] - out["fp64"][0]) <= 1e-7 * abs(out["fp64"][0]), (lam, out)
+
+
+def test_tile_policy_does_not_change_results():
+    """The 64 x 64 and 32 x 32 tile kernels add in the same order: any tile policy gives the same bits."""
+    import torch
+
+    from autojax_gb300 import _lib, tune
+
+    lib = _lib.load()
+    S = 700
+    A = torch.from_numpy(_spd_with_condition(S, 1e5, 11)).cuda()
+    ws = torch.empty(lib.aj_spd_inverse_mixed_workspace_size(S), dtype=torch.uint8, device="cuda")
+    saved = tune.get_tile_policy()
+    outs = []
+    try:
+        for pol in ((1, 1, 1), (tune.NEVER,) * 3, (40, 200, 20)):
+            tune.set_tile_policy(*pol)
+            inv = torch.empty_like(A)
+            ld = torch.zeros(1, dtype=torch.float64, device="cuda")
+            info = torch.zeros(2, dtype=torch.int32, device="cuda")
+            _lib.check(lib.aj_spd_inverse_mixed(A.data_ptr(), S, inv.data_ptr(), ld.data_ptr(), ws.data_ptr(),
+                                                ws.numel(), info.data_ptr(), torch.cuda.current_stream().cuda_stream),
+                       "aj_spd_inverse_mixed")
+            torch.cuda.synchronize()
+            outs.append((inv.clone(), ld.clone()))
+    finally:
+        tune.set_tile_policy(*saved)
+    for inv, ld in outs[1:]:
+        assert torch.equal(inv, outs[0][0]) and torch.equal(ld, outs[0][1])
