@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--skip-batch", action="store_true", help="omit the batched many-model measurement")
     ap.add_argument("--batch", type=int, default=64, help="lens models in the batched measurement")
     ap.add_argument("--only", choices=("roofline", "wtilde"), help="run one kernel measurement alone (for ncu)")
+    ap.add_argument("--tile-policy", help="fixed tile policy 'update,inverse,lauum' instead of tuning (for ncu)")
     return ap.parse_args()
 
 
@@ -309,6 +310,10 @@ def roofline_only(args, dist: Dist) -> dict:
     import torch
 
     torch.cuda.set_device(dist.local)
+    if args.tile_policy:
+        from autojax_gb300 import tune
+
+        tune.set_tile_policy(*(int(v) for v in args.tile_policy.split(",")))
     S = 1500
     rng = np.random.default_rng(3)
     X = rng.standard_normal((S, S))
@@ -346,7 +351,11 @@ def gpu_arm(args, dist: Dist) -> dict:
     # tile shapes of the double-float factorisation, chosen by timing this evaluation
     from autojax_gb300 import tune
 
-    tuned = tune.tune_tile_policy(ev["mixed"].launch)
+    if args.tile_policy:
+        tune.set_tile_policy(*(int(v) for v in args.tile_policy.split(",")))
+        tuned = {"policy": tune.get_tile_policy(), "ms": None, "ms_default": None, "candidates_timed": 0}
+    else:
+        tuned = tune.tune_tile_policy(ev["mixed"].launch)
     for e in ev.values():
         if not args.no_graph:
             e.capture()

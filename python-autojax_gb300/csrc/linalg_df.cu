@@ -304,7 +304,8 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 // panel's rows), so the critical chain is one launch per step; the rest of
 // each trailing update runs on another lane.
 constexpr int PANEL_THREADS = 512;
-constexpr size_t PANEL_DYN_SMEM = sizeof(float) * 2 * 64 * (32 + 1);  // previous-panel rows of this block
+// previous-panel rows as (hi, lo) pairs: the pivot block's 32 and this block's 64
+constexpr size_t PANEL_DYN_SMEM = sizeof(float2) * (32 + 64) * (32 + 1);
 
 __global__ void __launch_bounds__(PANEL_THREADS)
     dfchol_panel_kernel(DfMats mats, int64_t S, int64_t k0, int pre, int* info) {
@@ -323,9 +324,9 @@ __global__ void __launch_bounds__(PANEL_THREADS)
     __shared__ float rh[DNB], rl[DNB];
     __shared__ float th[DNB * DNB / 4], tl[DNB * DNB / 4];
     __shared__ float xh[64][DNB + 1], xl[64][DNB + 1];
-    extern __shared__ float panel_dyn[];
-    float(*prh)[DNB + 1] = reinterpret_cast<float(*)[DNB + 1]>(panel_dyn);
-    float(*prl)[DNB + 1] = reinterpret_cast<float(*)[DNB + 1]>(panel_dyn + 64 * (DNB + 1));
+    extern __shared__ float2 panel_dyn[];
+    float2(*pdf)[DNB + 1] = reinterpret_cast<float2(*)[DNB + 1]>(panel_dyn);                    // P_k: 32 rows
+    float2(*prf)[DNB + 1] = reinterpret_cast<float2(*)[DNB + 1]>(panel_dyn + DNB * (DNB + 1));  // P_r: 64 rows
     __shared__ int bad;
     const int tid = threadIdx.x;
     const int64_t nb = (S - k0) < DNB ? (S - k0) : DNB;
@@ -344,10 +345,12 @@ __global__ void __launch_bounds__(PANEL_THREADS)
         }
         ah[i][j] = vh;
         al[i][j] = vl;
-        // with pre, ih/il first hold the previous panel's pivot-block rows P_k
-        const bool pin = pre && i < nb;
-        ih[i][j] = pin ? Lh[(k0 + i) * S + kp + j] : 0.f;
-        il[i][j] = pin ? Ll[(k0 + i) * S + kp + j] : 0.f;
+        if (pre) {
+            const bool pin = i < nb;
+            pdf[i][j] = pin ? make_float2(Lh[(k0 + i) * S + kp + j], Ll[(k0 + i) * S + kp + j]) : make_float2(0.f, 0.f);
+        }
+        ih[i][j] = 0.f;
+        il[i][j] = 0.f;
         lh[i][j] = 0.f;
         ll[i][j] = 0.f;
     }
@@ -360,45 +363,54 @@ __global__ void __launch_bounds__(PANEL_THREADS)
             const bool in = r < S && j < nb;
             xh[i][j] = in ? Lh[r * S + k0 + j] : 0.f;
             xl[i][j] = in ? Ll[r * S + k0 + j] : 0.f;
-            if (pre) {
-                prh[i][j] = r < S ? Lh[r * S + kp + j] : 0.f;
-                prl[i][j] = r < S ? Ll[r * S + kp + j] : 0.f;
-            }
+            if (pre) prf[i][j] = r < S ? make_float2(Lh[r * S + kp + j], Ll[r * S + kp + j]) : make_float2(0.f, 0.f);
         }
     }
     __syncthreads();
     if (pre) {
-        // A_kk (lower) -= P_k P_k^T and rows -= P_r P_k^T: element (i, j) sums p over the 32 previous columns
-        const int nout = DNB * DNB + (blockIdx.x > 0 ? 64 * DNB : 0);
-        for (int o = tid; o < nout; o += PANEL_THREADS) {
-            const bool diag = o < DNB * DNB;
-            const int i = diag ? o / DNB : (o - DNB * DNB) / DNB, j = o % DNB;
-            if (diag && j > i) continue;
-            df acc = {0.f, 0.f};
+        // A_kk (lower) -= P_k P_k^T and rows -= P_r P_k^T; element (i, j) sums q over the 32 previous
+        // columns.  Thread (r, c) owns rows r (pivot block), r and r + 32 (panel rows) and columns c,
+        // c + 16: five (hi, lo) loads feed six multiply-adds per q.
+        const int r = tid >> 4, c = tid & 15;
+        const bool rows = blockIdx.x > 0;
+        df acc[3][2] = {{{0.f, 0.f}, {0.f, 0.f}}, {{0.f, 0.f}, {0.f, 0.f}}, {{0.f, 0.f}, {0.f, 0.f}}};
 #pragma unroll 8
-            for (int q = 0; q < DNB; ++q) {
-                const df x = diag ? df{ih[i][q], il[i][q]} : df{prh[i][q], prl[i][q]};
-                df_fma_lazy(acc, x, {ih[j][q], il[j][q]});
-                if ((q & 7) == 7) df_renorm(acc);
+        for (int q = 0; q < DNB; ++q) {
+            const float2 y0 = pdf[c][q], y1 = pdf[c + 16][q];
+            const float2 x0 = pdf[r][q];
+            df_fma_lazy(acc[0][0], {x0.x, x0.y}, {y0.x, y0.y});
+            df_fma_lazy(acc[0][1], {x0.x, x0.y}, {y1.x, y1.y});
+            if (rows) {
+                const float2 x1 = prf[r][q], x2 = prf[r + 32][q];
+                df_fma_lazy(acc[1][0], {x1.x, x1.y}, {y0.x, y0.y});
+                df_fma_lazy(acc[1][1], {x1.x, x1.y}, {y1.x, y1.y});
+                df_fma_lazy(acc[2][0], {x2.x, x2.y}, {y0.x, y0.y});
+                df_fma_lazy(acc[2][1], {x2.x, x2.y}, {y1.x, y1.y});
             }
-            if (diag) {
-                if (i < nb && j < nb) {
-                    const df v = df_add({ah[i][j], al[i][j]}, df_neg(acc));
-                    ah[i][j] = v.hi;
-                    al[i][j] = v.lo;
+            if ((q & 7) == 7)
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    df_renorm(acc[a][0]);
+                    df_renorm(acc[a][1]);
                 }
-            } else {
-                const df v = df_add({xh[i][j], xl[i][j]}, df_neg(acc));
-                xh[i][j] = v.hi;
-                xl[i][j] = v.lo;
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int j = c + 16 * h;
+            if (j <= r && r < nb && j < nb) {
+                const df v = df_add({ah[r][j], al[r][j]}, df_neg(acc[0][h]));
+                ah[r][j] = v.hi;
+                al[r][j] = v.lo;
+            }
+            if (rows) {
+                const df v1 = df_add({xh[r][j], xl[r][j]}, df_neg(acc[1][h]));
+                xh[r][j] = v1.hi;
+                xl[r][j] = v1.lo;
+                const df v2 = df_add({xh[r + 32][j], xl[r + 32][j]}, df_neg(acc[2][h]));
+                xh[r + 32][j] = v2.hi;
+                xl[r + 32][j] = v2.lo;
             }
         }
-        __syncthreads();
-        for (int e = tid; e < DNB * DNB; e += PANEL_THREADS) {
-            ih[e / DNB][e % DNB] = 0.f;
-            il[e / DNB][e % DNB] = 0.f;
-        }
-        __syncthreads();
     }
     const int ur = tid >> 4, uq = tid & 15;  // update: row ur, columns uq and uq + 16
     // one barrier a column: every thread evaluates the pivot itself; the scaled
@@ -413,8 +425,9 @@ __global__ void __launch_bounds__(PANEL_THREADS)
             }
             break;
         }
+        if (ur < j) continue;  // rows above the pivot are finished (whole warps once j > 2 w + 1)
         const df rj = dfrsqrt(d);
-        if (tid == 0) {
+        if (ur == j && uq == 0) {
             const df l = dfmul(d, rj);
             lh[j][j] = l.hi;
             ll[j][j] = l.lo;

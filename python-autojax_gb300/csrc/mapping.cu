@@ -108,7 +108,7 @@ __device__ __forceinline__ bool csc_entry(const int64_t* idx, const int64_t* siz
 // each column, and each chunk then writes its entries in order.  Columns come
 // out sorted by (m, b) — the reference's loop order — with no atomics on the
 // output and no per-column sort, whatever the column lengths.
-constexpr int CSC_CHUNK = 1024;
+constexpr int CSC_CHUNK = 256;
 
 __global__ void __launch_bounds__(256)
     csc_hist_kernel(const int64_t* __restrict__ idx, const int64_t* __restrict__ sizes, int64_t M, int64_t B,
@@ -134,8 +134,10 @@ __global__ void csc_offsets_kernel(const int* __restrict__ hist, int64_t nchunk,
     for (int64_t s0 = 0; s0 < S; s0 += blockDim.x) {
         const int64_t s = s0 + threadIdx.x;
         int tot = 0;
-        if (s < S)
+        if (s < S) {
+#pragma unroll 8
             for (int64_t c = 0; c < nchunk; ++c) tot += hist[c * S + s];
+        }
         int x = tot;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -149,6 +151,7 @@ __global__ void csc_offsets_kernel(const int* __restrict__ hist, int64_t nchunk,
         if (s < S) {
             int run = base + before + x - tot;
             colptr[s] = run;
+#pragma unroll 8
             for (int64_t c = 0; c < nchunk; ++c) {
                 off[c * S + s] = run;
                 run += hist[c * S + s];
