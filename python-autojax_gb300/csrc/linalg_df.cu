@@ -303,7 +303,10 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 // own block column (A_kk -= P_k P_k^T, rows -= P_r P_k^T with P the previous
 // panel's rows), so the critical chain is one launch per step; the rest of
 // each trailing update runs on another lane.
-constexpr int PANEL_THREADS = 512;
+constexpr int PANEL_THREADS = 1024;
+constexpr int PANEL_RT = PANEL_THREADS / DNB;  // threads per row in the factor loop and the pre-update
+constexpr int PANEL_NC = DNB / PANEL_RT;       // columns per thread there
+constexpr int PANEL_CPW = DNB / (PANEL_THREADS / 32);  // columns per warp in the panel product
 // previous-panel rows as (hi, lo) pairs: the pivot block's 32 and this block's 64
 constexpr size_t PANEL_DYN_SMEM = sizeof(float2) * (32 + 64) * (32 + 1);
 
@@ -371,32 +374,38 @@ __global__ void __launch_bounds__(PANEL_THREADS)
         // A_kk (lower) -= P_k P_k^T and rows -= P_r P_k^T; element (i, j) sums q over the 32 previous
         // columns.  Thread (r, c) owns rows r (pivot block), r and r + 32 (panel rows) and columns c,
         // c + 16: five (hi, lo) loads feed six multiply-adds per q.
-        const int r = tid >> 4, c = tid & 15;
+        const int r = tid / PANEL_RT, c = tid % PANEL_RT;
         const bool rows = blockIdx.x > 0;
-        df acc[3][2] = {{{0.f, 0.f}, {0.f, 0.f}}, {{0.f, 0.f}, {0.f, 0.f}}, {{0.f, 0.f}, {0.f, 0.f}}};
+        df acc[3][PANEL_NC];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int h = 0; h < PANEL_NC; ++h) acc[a][h] = {0.f, 0.f};
 #pragma unroll 8
         for (int q = 0; q < DNB; ++q) {
-            const float2 y0 = pdf[c][q], y1 = pdf[c + 16][q];
+            float2 y[PANEL_NC];
+#pragma unroll
+            for (int h = 0; h < PANEL_NC; ++h) y[h] = pdf[c + PANEL_RT * h][q];
             const float2 x0 = pdf[r][q];
-            df_fma_lazy(acc[0][0], {x0.x, x0.y}, {y0.x, y0.y});
-            df_fma_lazy(acc[0][1], {x0.x, x0.y}, {y1.x, y1.y});
+#pragma unroll
+            for (int h = 0; h < PANEL_NC; ++h) df_fma_lazy(acc[0][h], {x0.x, x0.y}, {y[h].x, y[h].y});
             if (rows) {
                 const float2 x1 = prf[r][q], x2 = prf[r + 32][q];
-                df_fma_lazy(acc[1][0], {x1.x, x1.y}, {y0.x, y0.y});
-                df_fma_lazy(acc[1][1], {x1.x, x1.y}, {y1.x, y1.y});
-                df_fma_lazy(acc[2][0], {x2.x, x2.y}, {y0.x, y0.y});
-                df_fma_lazy(acc[2][1], {x2.x, x2.y}, {y1.x, y1.y});
+#pragma unroll
+                for (int h = 0; h < PANEL_NC; ++h) {
+                    df_fma_lazy(acc[1][h], {x1.x, x1.y}, {y[h].x, y[h].y});
+                    df_fma_lazy(acc[2][h], {x2.x, x2.y}, {y[h].x, y[h].y});
+                }
             }
             if ((q & 7) == 7)
 #pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    df_renorm(acc[a][0]);
-                    df_renorm(acc[a][1]);
-                }
+                for (int a = 0; a < 3; ++a)
+#pragma unroll
+                    for (int h = 0; h < PANEL_NC; ++h) df_renorm(acc[a][h]);
         }
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int j = c + 16 * h;
+        for (int h = 0; h < PANEL_NC; ++h) {
+            const int j = c + PANEL_RT * h;
             if (j <= r && r < nb && j < nb) {
                 const df v = df_add({ah[r][j], al[r][j]}, df_neg(acc[0][h]));
                 ah[r][j] = v.hi;
@@ -412,7 +421,7 @@ __global__ void __launch_bounds__(PANEL_THREADS)
             }
         }
     }
-    const int ur = tid >> 4, uq = tid & 15;  // update: row ur, columns uq and uq + 16
+    const int ur = tid / PANEL_RT, uq = tid % PANEL_RT;  // update: row ur, columns uq, uq + PANEL_RT, ...
     // one barrier a column: every thread evaluates the pivot itself; the scaled
     // column goes to L (lh/ll) so the update can keep reading the unscaled one
     for (int j = 0; j < DNB; ++j) {
@@ -442,7 +451,7 @@ __global__ void __launch_bounds__(PANEL_THREADS)
                 ll[ur][j] = lrj.lo;
             }
 #pragma unroll
-            for (int c = uq; c < DNB; c += 16)
+            for (int c = uq; c < DNB; c += PANEL_RT)
                 if (c > j && c <= ur) {
                     const df lcj = dfmul({ah[c][j], al[c][j]}, rj);
                     df v = {ah[ur][c], al[ur][c]};
@@ -502,11 +511,11 @@ __global__ void __launch_bounds__(PANEL_THREADS)
         }
         return;
     }
-    // out[row][c] = sum_{p <= c} x[row][p] X[c][p]: warp w takes columns w and
-    // 31 - w, lane l rows l and l + 32
+    // out[row][c] = sum_{p <= c} x[row][p] X[c][p]: with 16 warps warp w takes columns w and
+    // 31 - w (equal total length), with 32 warps column w; lane l rows l and l + 32
     const int w = tid >> 5, lane = tid & 31;
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < PANEL_CPW; ++h) {
         const int c = h == 0 ? w : DNB - 1 - w;
         df o0 = {0.f, 0.f}, o1 = {0.f, 0.f};
         for (int p0 = 0; p0 <= c; p0 += 8) {
