@@ -355,7 +355,10 @@ def gpu_arm(args, dist: Dist) -> dict:
         tune.set_tile_policy(*(int(v) for v in args.tile_policy.split(",")))
         tuned = {"policy": tune.get_tile_policy(), "ms": None, "ms_default": None, "candidates_timed": 0}
     else:
-        tuned = tune.tune_tile_policy(ev["mixed"].launch)
+        # timed as graph replays when the bench replays graphs (a graph keeps its capture's policy)
+        em = ev["mixed"]
+        tuned = (tune.tune_tile_policy(em.launch) if args.no_graph
+                 else tune.tune_tile_policy(em.step, prepare=em.capture))
     for e in ev.values():
         if not args.no_graph:
             e.capture()
