@@ -285,28 +285,23 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 
 // -------------------------------------------------------------- Cholesky
 
-// Factor + invert the diagonal block at k0 (every block, redundantly), then:
-// block 0 stores L_kk (in the factored-block buffer, not in L: blocks of the
-// same launch may start late and must still read the unfactored block from
-// L), its inverse and the pivots; block b >= 1 replaces the 64 panel rows
-// k0 + 32 + 64 (b - 1) .. by A_rows L_kk^-T.
+// Factor the diagonal block at k0 (every block, redundantly) and, in block
+// b >= 1, solve the 64 panel rows k0 + 32 + 64 (b - 1) .. for L's columns
+// (rows <- A_rows L_kk^-T) in the same column loop.  Block 0 stores L_kk (in
+// the factored-block buffer, not in L: blocks of the same launch may start
+// late and must still read the unfactored block from L), the pivots and
+// L_kk^-1, which it computes while the other blocks solve their rows.
 // Latency matters more than work here (one launch per 32 columns sits on the
-// critical path), so the kernel keeps its barrier count and its per-warp
-// instruction count low:
-//  - factor: one barrier a column; every thread evaluates the pivot itself and
-//    the column scaling is fused into the rank-1 update;
-//  - inverse: recursive doubling, 5 levels of two small products each
-//    (inv [[A, 0], [B, C]] = [[A^-1, 0], [-C^-1 B A^-1, C^-1]]);
-//  - panel product: each warp owns two columns whose triangular dot-product
-//    lengths add to 33, so all lanes of a warp run the same loop.
+// critical path), so the column loop takes one barrier a column and lets each
+// finished column's warp drop out.
 // With `pre` set the kernel first applies the previous step's update to its
 // own block column (A_kk -= P_k P_k^T, rows -= P_r P_k^T with P the previous
 // panel's rows), so the critical chain is one launch per step; the rest of
 // each trailing update runs on another lane.
 constexpr int PANEL_THREADS = 1024;
-constexpr int PANEL_RT = PANEL_THREADS / DNB;  // threads per row in the factor loop and the pre-update
+constexpr int PANEL_RT = PANEL_THREADS / DNB;  // threads per row in the pre-update
 constexpr int PANEL_NC = DNB / PANEL_RT;       // columns per thread there
-constexpr int PANEL_CPW = DNB / (PANEL_THREADS / 32);  // columns per warp in the panel product
+static_assert(PANEL_THREADS == 32 * DNB, "the panel column loop gives each column its own warp");
 // previous-panel rows as (hi, lo) pairs: the pivot block's 32 and this block's 64
 constexpr size_t PANEL_DYN_SMEM = sizeof(float2) * (32 + 64) * (32 + 1);
 
@@ -322,8 +317,7 @@ __global__ void __launch_bounds__(PANEL_THREADS)
     float* __restrict__ fl = pick(mats.fl, z) + kb * DNB * DNB;
     double* __restrict__ piv = pick(mats.piv, z);
     __shared__ float ah[DNB][DNB + 1], al[DNB][DNB + 1];
-    __shared__ float ih[DNB][DNB + 1], il[DNB][DNB + 1];
-    __shared__ float lh[DNB][DNB + 1], ll[DNB][DNB + 1];
+    __shared__ float ih[DNB][DNB + 1], il[DNB][DNB + 1];  // L_kk^-1 (block 0)
     __shared__ float rh[DNB], rl[DNB];
     __shared__ float th[DNB * DNB / 4], tl[DNB * DNB / 4];
     __shared__ float xh[64][DNB + 1], xl[64][DNB + 1];
@@ -352,10 +346,6 @@ __global__ void __launch_bounds__(PANEL_THREADS)
             const bool pin = i < nb;
             pdf[i][j] = pin ? make_float2(Lh[(k0 + i) * S + kp + j], Ll[(k0 + i) * S + kp + j]) : make_float2(0.f, 0.f);
         }
-        ih[i][j] = 0.f;
-        il[i][j] = 0.f;
-        lh[i][j] = 0.f;
-        ll[i][j] = 0.f;
     }
     // panel rows are loaded up front so their latency overlaps the factorisation
     const int64_t r0 = k0 + DNB + (int64_t)(blockIdx.x - 1) * 64;
@@ -421,80 +411,126 @@ __global__ void __launch_bounds__(PANEL_THREADS)
             }
         }
     }
-    const int ur = tid / PANEL_RT, uq = tid % PANEL_RT;  // update: row ur, columns uq, uq + PANEL_RT, ...
-    // one barrier a column: every thread evaluates the pivot itself; the scaled
-    // column goes to L (lh/ll) so the update can keep reading the unscaled one
-    for (int j = 0; j < DNB; ++j) {
-        __syncthreads();
-        const df d = {ah[j][j], al[j][j]};
+    // Factor the pivot block and solve the panel rows in one right-looking column loop, one
+    // barrier a column.  Warp c owns column c of every row: lane l holds pivot row l and panel
+    // rows l and l + 32.  Column j is scaled (L's column j) when step j starts; warp j + 1 applies
+    // it to column j + 1, takes that column's pivot and scales the column, while warps c > j + 1
+    // apply it to their columns.  Columns <= j are final, so their warps sit the step out.
+    const int w = tid >> 5, lane = tid & 31;
+    const bool rows = blockIdx.x > 0;
+    __syncthreads();  // the pre-update's writes
+    if (w == 0) {
+        const df d = {ah[0][0], al[0][0]};
         if (!(d.hi > 0.f)) {
-            if (tid == 0) {
+            if (lane == 0) {
                 bad = 1;
-                if (blockIdx.x == 0) report(info, AJ_INFO_NOT_POSITIVE_DEFINITE, k0 + j);
+                if (blockIdx.x == 0) report(info, AJ_INFO_NOT_POSITIVE_DEFINITE, k0);
             }
-            break;
-        }
-        if (ur < j) continue;  // rows above the pivot are finished (whole warps once j > 2 w + 1)
-        const df rj = dfrsqrt(d);
-        if (ur == j && uq == 0) {
-            const df l = dfmul(d, rj);
-            lh[j][j] = l.hi;
-            ll[j][j] = l.lo;
-            rh[j] = rj.hi;
-            rl[j] = rj.lo;
-            if (blockIdx.x == 0 && j < nb) piv[k0 + j] = df_to(l);
-        }
-        if (ur > j) {
-            const df lrj = dfmul({ah[ur][j], al[ur][j]}, rj);
-            if (uq == 0) {
-                lh[ur][j] = lrj.hi;
-                ll[ur][j] = lrj.lo;
+        } else {
+            const df r = dfrsqrt(d);
+            const df v = lane == 0 ? dfmul(d, r) : dfmul({ah[lane][0], al[lane][0]}, r);
+            ah[lane][0] = v.hi;
+            al[lane][0] = v.lo;
+            if (rows) {
+                const df v1 = dfmul({xh[lane][0], xl[lane][0]}, r), v2 = dfmul({xh[lane + 32][0], xl[lane + 32][0]}, r);
+                xh[lane][0] = v1.hi;
+                xl[lane][0] = v1.lo;
+                xh[lane + 32][0] = v2.hi;
+                xl[lane + 32][0] = v2.lo;
             }
-#pragma unroll
-            for (int c = uq; c < DNB; c += PANEL_RT)
-                if (c > j && c <= ur) {
-                    const df lcj = dfmul({ah[c][j], al[c][j]}, rj);
-                    df v = {ah[ur][c], al[ur][c]};
-                    df_fms_acc(v, lrj, lcj);
-                    ah[ur][c] = v.hi;
-                    al[ur][c] = v.lo;
+            if (lane == 0) {
+                rh[0] = r.hi;
+                rl[0] = r.lo;
+                if (blockIdx.x == 0) piv[k0] = df_to(v);
+            }
+        }
+    }
+    __syncthreads();
+    for (int j = 0; j + 1 < DNB; ++j) {
+        if (bad) break;
+        if (w > j) {
+            const int c = w;
+            const df lc = {ah[c][j], al[c][j]};
+            const bool low = lane >= c;  // pivot row lane, lower triangle
+            df v0 = {0.f, 0.f}, v1 = {0.f, 0.f}, v2 = {0.f, 0.f};
+            if (low) {
+                v0 = {ah[lane][c], al[lane][c]};
+                df_fms_acc(v0, {ah[lane][j], al[lane][j]}, lc);
+            }
+            if (rows) {
+                v1 = {xh[lane][c], xl[lane][c]};
+                df_fms_acc(v1, {xh[lane][j], xl[lane][j]}, lc);
+                v2 = {xh[lane + 32][c], xl[lane + 32][c]};
+                df_fms_acc(v2, {xh[lane + 32][j], xl[lane + 32][j]}, lc);
+            }
+            if (c == j + 1) {
+                const df d = {__shfl_sync(0xffffffffu, v0.hi, c), __shfl_sync(0xffffffffu, v0.lo, c)};
+                if (!(d.hi > 0.f)) {
+                    if (lane == 0) {
+                        bad = 1;
+                        if (blockIdx.x == 0) report(info, AJ_INFO_NOT_POSITIVE_DEFINITE, k0 + c);
+                    }
+                } else {
+                    const df r = dfrsqrt(d);
+                    if (low) v0 = lane == c ? dfmul(d, r) : dfmul(v0, r);
+                    if (rows) {
+                        v1 = dfmul(v1, r);
+                        v2 = dfmul(v2, r);
+                    }
+                    if (lane == c) {
+                        rh[c] = r.hi;
+                        rl[c] = r.lo;
+                        if (blockIdx.x == 0 && c < nb) piv[k0 + c] = df_to(v0);
+                    }
                 }
+            }
+            if (low) {
+                ah[lane][c] = v0.hi;
+                al[lane][c] = v0.lo;
+            }
+            if (rows) {
+                xh[lane][c] = v1.hi;
+                xl[lane][c] = v1.lo;
+                xh[lane + 32][c] = v2.hi;
+                xl[lane + 32][c] = v2.lo;
+            }
         }
+        __syncthreads();
     }
-    __syncthreads();
     if (bad) return;
-    // inverse X = L^-1 by recursive doubling: at level b the 32 / (2b) pairs of
-    // b x b diagonal blocks (A above C, B the block of L between them) get
-    // their off-diagonal block -C^-1 (B A^-1), through T = B A^-1 in th/tl
-    if (tid < DNB) {
-        ih[tid][tid] = rh[tid];
-        il[tid][tid] = rl[tid];
-    }
-    __syncthreads();
-    for (int b = 1; b < DNB; b <<= 1) {
-        const int n = (DNB / 2) * b;  // outputs of this level: pairs x b^2
-        const int pair = tid / (b * b), rem = tid % (b * b), r = rem / b, c = rem % b;
-        const int i0 = 2 * b * pair;
-        if (tid < n) {
-            df acc = {0.f, 0.f};
-            for (int q = c; q < b; ++q)
-                df_fma_acc(acc, {lh[i0 + b + r][i0 + q], ll[i0 + b + r][i0 + q]},
-                           {ih[i0 + q][i0 + c], il[i0 + q][i0 + c]});
-            th[tid] = acc.hi;
-            tl[tid] = acc.lo;
-        }
-        __syncthreads();
-        if (tid < n) {
-            df acc = {0.f, 0.f};
-            for (int q = 0; q <= r; ++q)
-                df_fma_acc(acc, {ih[i0 + b + r][i0 + b + q], il[i0 + b + r][i0 + b + q]},
-                           {th[pair * b * b + q * b + c], tl[pair * b * b + q * b + c]});
-            ih[i0 + b + r][i0 + c] = -acc.hi;
-            il[i0 + b + r][i0 + c] = -acc.lo;
-        }
-        __syncthreads();
-    }
     if (blockIdx.x == 0) {
+        // L_kk^-1 by recursive doubling while the other blocks solve and store their rows: at
+        // level b the 32 / (2b) pairs of b x b diagonal blocks (A above C, B the block of L
+        // between them) get their off-diagonal block -C^-1 (B A^-1), through T = B A^-1
+        for (int e = tid; e < DNB * DNB; e += PANEL_THREADS) {
+            const int i = e / DNB, j = e % DNB;
+            ih[i][j] = i == j ? rh[i] : 0.f;
+            il[i][j] = i == j ? rl[i] : 0.f;
+        }
+        __syncthreads();
+        for (int b = 1; b < DNB; b <<= 1) {
+            const int n = (DNB / 2) * b;  // outputs of this level: pairs x b^2
+            const int pair = tid / (b * b), rem = tid % (b * b), r = rem / b, c = rem % b;
+            const int i0 = 2 * b * pair;
+            if (tid < n) {
+                df acc = {0.f, 0.f};
+                for (int q = c; q < b; ++q)
+                    df_fma_acc(acc, {ah[i0 + b + r][i0 + q], al[i0 + b + r][i0 + q]},
+                               {ih[i0 + q][i0 + c], il[i0 + q][i0 + c]});
+                th[tid] = acc.hi;
+                tl[tid] = acc.lo;
+            }
+            __syncthreads();
+            if (tid < n) {
+                df acc = {0.f, 0.f};
+                for (int q = 0; q <= r; ++q)
+                    df_fma_acc(acc, {ih[i0 + b + r][i0 + b + q], il[i0 + b + r][i0 + b + q]},
+                               {th[pair * b * b + q * b + c], tl[pair * b * b + q * b + c]});
+                ih[i0 + b + r][i0 + c] = -acc.hi;
+                il[i0 + b + r][i0 + c] = -acc.lo;
+            }
+            __syncthreads();
+        }
         float* __restrict__ Ih = z < mats.ninv ? pick(mats.Ih, z) : nullptr;
         float* __restrict__ Il = z < mats.ninv ? pick(mats.Il, z) : nullptr;
         for (int e = tid; e < DNB * DNB; e += PANEL_THREADS) {
@@ -504,40 +540,19 @@ __global__ void __launch_bounds__(PANEL_THREADS)
                 Ih[off] = ih[i][j];
                 Il[off] = il[i][j];
             }
-            fh[e] = j <= i ? lh[i][j] : 0.f;
-            fl[e] = j <= i ? ll[i][j] : 0.f;
+            fh[e] = j <= i ? ah[i][j] : 0.f;
+            fl[e] = j <= i ? al[i][j] : 0.f;
             dh[e] = ih[i][j];
             dl[e] = il[i][j];
         }
         return;
     }
-    // out[row][c] = sum_{p <= c} x[row][p] X[c][p]: with 16 warps warp w takes columns w and
-    // 31 - w (equal total length), with 32 warps column w; lane l rows l and l + 32
-    const int w = tid >> 5, lane = tid & 31;
-#pragma unroll
-    for (int h = 0; h < PANEL_CPW; ++h) {
-        const int c = h == 0 ? w : DNB - 1 - w;
-        df o0 = {0.f, 0.f}, o1 = {0.f, 0.f};
-        for (int p0 = 0; p0 <= c; p0 += 8) {
-            const int p1 = p0 + 8 <= c + 1 ? p0 + 8 : c + 1;
-            for (int p = p0; p < p1; ++p) {
-                const df y = {ih[c][p], il[c][p]};
-                df_fma_lazy(o0, {xh[lane][p], xl[lane][p]}, y);
-                df_fma_lazy(o1, {xh[lane + 32][p], xl[lane + 32][p]}, y);
-            }
-            df_renorm(o0);
-            df_renorm(o1);
-        }
-        if (c < nb) {
-            const int64_t ra = r0 + lane, rb = r0 + lane + 32;
-            if (ra < S) {
-                Lh[ra * S + k0 + c] = o0.hi;
-                Ll[ra * S + k0 + c] = o0.lo;
-            }
-            if (rb < S) {
-                Lh[rb * S + k0 + c] = o1.hi;
-                Ll[rb * S + k0 + c] = o1.lo;
-            }
+    for (int e = tid; e < 64 * DNB; e += PANEL_THREADS) {
+        const int i = e / DNB, j = e % DNB;
+        const int64_t r = r0 + i;
+        if (r < S && j < nb) {
+            Lh[r * S + k0 + j] = xh[i][j];
+            Ll[r * S + k0 + j] = xl[i][j];
         }
     }
 }
