@@ -34,7 +34,7 @@ struct DfMats {
     float* fh[2];  // factored diagonal blocks (copied into L after the last panel)
     float* fl[2];
     double* piv[2];
-    int ninv;  // matrices z < ninv also get L^-1: the panel writes its diagonal block
+    int ninv;  // matrices z < ninv also get L^-1: df_diag_inverse_kernel writes its diagonal blocks
 };
 
 // element z of a kernel-parameter pair without indexing it dynamically (which
@@ -289,8 +289,9 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 // b >= 1, solve the 64 panel rows k0 + 32 + 64 (b - 1) .. for L's columns
 // (rows <- A_rows L_kk^-T) in the same column loop.  Block 0 stores L_kk (in
 // the factored-block buffer, not in L: blocks of the same launch may start
-// late and must still read the unfactored block from L), the pivots and
-// L_kk^-1, which it computes while the other blocks solve their rows.
+// late and must still read the unfactored block from L), the pivots and the
+// inverse's diagonal 1 / l_jj; df_diag_inverse_kernel completes L_kk^-1 on a
+// lane of its own, off the critical chain.
 // Latency matters more than work here (one launch per 32 columns sits on the
 // critical path), so the column loop takes one barrier a column and lets each
 // finished column's warp drop out.
@@ -301,7 +302,8 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 constexpr int PANEL_THREADS = 1024;
 constexpr int PANEL_RT = PANEL_THREADS / DNB;  // threads per row in the pre-update
 constexpr int PANEL_NC = DNB / PANEL_RT;       // columns per thread there
-static_assert(PANEL_THREADS == 32 * DNB, "the panel column loop gives each column its own warp");
+constexpr int PANEL_SP = 8;  // sub-panel width of the panel factorisation
+static_assert(PANEL_THREADS == 32 * DNB && DNB % PANEL_SP == 0, "the pre-update gives each thread one column");
 // previous-panel rows as (hi, lo) pairs: the pivot block's 32 and this block's 64
 constexpr size_t PANEL_DYN_SMEM = sizeof(float2) * (32 + 64) * (32 + 1);
 
@@ -316,16 +318,16 @@ __global__ void __launch_bounds__(PANEL_THREADS)
     float* __restrict__ fh = pick(mats.fh, z) + kb * DNB * DNB;
     float* __restrict__ fl = pick(mats.fl, z) + kb * DNB * DNB;
     double* __restrict__ piv = pick(mats.piv, z);
-    __shared__ float ah[DNB][DNB + 1], al[DNB][DNB + 1];
-    __shared__ float ih[DNB][DNB + 1], il[DNB][DNB + 1];  // L_kk^-1 (block 0)
+    // the block's rows: 0 .. 31 the pivot block (lower triangle), 32 .. 95 the panel rows
+    __shared__ float ph[3 * DNB][DNB + 1], pl[3 * DNB][DNB + 1];
     __shared__ float rh[DNB], rl[DNB];
-    __shared__ float th[DNB * DNB / 4], tl[DNB * DNB / 4];
-    __shared__ float xh[64][DNB + 1], xl[64][DNB + 1];
     extern __shared__ float2 panel_dyn[];
     float2(*pdf)[DNB + 1] = reinterpret_cast<float2(*)[DNB + 1]>(panel_dyn);                    // P_k: 32 rows
     float2(*prf)[DNB + 1] = reinterpret_cast<float2(*)[DNB + 1]>(panel_dyn + DNB * (DNB + 1));  // P_r: 64 rows
     __shared__ int bad;
     const int tid = threadIdx.x;
+    const bool rows = blockIdx.x > 0;
+    const int nrow = rows ? 3 * DNB : DNB;
     const int64_t nb = (S - k0) < DNB ? (S - k0) : DNB;
     const int64_t kp = k0 - DNB;  // the previous panel's first column (pre only)
     if (tid == 0) bad = 0;
@@ -340,8 +342,8 @@ __global__ void __launch_bounds__(PANEL_THREADS)
             vh = i == j ? 1.f : 0.f;
             vl = 0.f;
         }
-        ah[i][j] = vh;
-        al[i][j] = vl;
+        ph[i][j] = vh;
+        pl[i][j] = vl;
         if (pre) {
             const bool pin = i < nb;
             pdf[i][j] = pin ? make_float2(Lh[(k0 + i) * S + kp + j], Ll[(k0 + i) * S + kp + j]) : make_float2(0.f, 0.f);
@@ -349,23 +351,22 @@ __global__ void __launch_bounds__(PANEL_THREADS)
     }
     // panel rows are loaded up front so their latency overlaps the factorisation
     const int64_t r0 = k0 + DNB + (int64_t)(blockIdx.x - 1) * 64;
-    if (blockIdx.x > 0) {
+    if (rows) {
         for (int e = tid; e < 64 * DNB; e += PANEL_THREADS) {
             const int i = e / DNB, j = e % DNB;
             const int64_t r = r0 + i;
             const bool in = r < S && j < nb;
-            xh[i][j] = in ? Lh[r * S + k0 + j] : 0.f;
-            xl[i][j] = in ? Ll[r * S + k0 + j] : 0.f;
+            ph[DNB + i][j] = in ? Lh[r * S + k0 + j] : 0.f;
+            pl[DNB + i][j] = in ? Ll[r * S + k0 + j] : 0.f;
             if (pre) prf[i][j] = r < S ? make_float2(Lh[r * S + kp + j], Ll[r * S + kp + j]) : make_float2(0.f, 0.f);
         }
     }
     __syncthreads();
     if (pre) {
         // A_kk (lower) -= P_k P_k^T and rows -= P_r P_k^T; element (i, j) sums q over the 32 previous
-        // columns.  Thread (r, c) owns rows r (pivot block), r and r + 32 (panel rows) and columns c,
-        // c + 16: five (hi, lo) loads feed six multiply-adds per q.
+        // columns.  Thread (r, c) owns rows r (pivot block), r and r + 32 (panel rows) and column c:
+        // four (hi, lo) loads feed three multiply-adds per q.
         const int r = tid / PANEL_RT, c = tid % PANEL_RT;
-        const bool rows = blockIdx.x > 0;
         df acc[3][PANEL_NC];
 #pragma unroll
         for (int a = 0; a < 3; ++a)
@@ -397,153 +398,111 @@ __global__ void __launch_bounds__(PANEL_THREADS)
         for (int h = 0; h < PANEL_NC; ++h) {
             const int j = c + PANEL_RT * h;
             if (j <= r && r < nb && j < nb) {
-                const df v = df_add({ah[r][j], al[r][j]}, df_neg(acc[0][h]));
-                ah[r][j] = v.hi;
-                al[r][j] = v.lo;
+                const df v = df_add({ph[r][j], pl[r][j]}, df_neg(acc[0][h]));
+                ph[r][j] = v.hi;
+                pl[r][j] = v.lo;
             }
             if (rows) {
-                const df v1 = df_add({xh[r][j], xl[r][j]}, df_neg(acc[1][h]));
-                xh[r][j] = v1.hi;
-                xl[r][j] = v1.lo;
-                const df v2 = df_add({xh[r + 32][j], xl[r + 32][j]}, df_neg(acc[2][h]));
-                xh[r + 32][j] = v2.hi;
-                xl[r + 32][j] = v2.lo;
+                const df v1 = df_add({ph[DNB + r][j], pl[DNB + r][j]}, df_neg(acc[1][h]));
+                ph[DNB + r][j] = v1.hi;
+                pl[DNB + r][j] = v1.lo;
+                const df v2 = df_add({ph[DNB + r + 32][j], pl[DNB + r + 32][j]}, df_neg(acc[2][h]));
+                ph[DNB + r + 32][j] = v2.hi;
+                pl[DNB + r + 32][j] = v2.lo;
             }
         }
     }
-    // Factor the pivot block and solve the panel rows in one right-looking column loop, one
-    // barrier a column.  Warp c owns column c of every row: lane l holds pivot row l and panel
-    // rows l and l + 32.  Column j is scaled (L's column j) when step j starts; warp j + 1 applies
-    // it to column j + 1, takes that column's pivot and scales the column, while warps c > j + 1
-    // apply it to their columns.  Columns <= j are final, so their warps sit the step out.
+    // Factor the pivot block and solve the panel rows for L's columns, 8 columns (a sub-panel)
+    // at a time.  Warps 0 .. 2 take a sub-panel through in registers, without block barriers:
+    // each holds the sub-panel's 8 x 8 diagonal block in lanes 0 .. 7 (factored identically by
+    // all three) and 32 of the block's rows, which it scales and updates as the columns pass.
+    // Meanwhile the other warps apply the previous sub-panel to the columns past the next
+    // sub-panel; then all warps apply this sub-panel to the next one.
     const int w = tid >> 5, lane = tid & 31;
-    const bool rows = blockIdx.x > 0;
-    __syncthreads();  // the pre-update's writes
-    if (w == 0) {
-        const df d = {ah[0][0], al[0][0]};
-        if (!(d.hi > 0.f)) {
-            if (lane == 0) {
-                bad = 1;
-                if (blockIdx.x == 0) report(info, AJ_INFO_NOT_POSITIVE_DEFINITE, k0);
-            }
-        } else {
-            const df r = dfrsqrt(d);
-            const df v = lane == 0 ? dfmul(d, r) : dfmul({ah[lane][0], al[lane][0]}, r);
-            ah[lane][0] = v.hi;
-            al[lane][0] = v.lo;
-            if (rows) {
-                const df v1 = dfmul({xh[lane][0], xl[lane][0]}, r), v2 = dfmul({xh[lane + 32][0], xl[lane + 32][0]}, r);
-                xh[lane][0] = v1.hi;
-                xl[lane][0] = v1.lo;
-                xh[lane + 32][0] = v2.hi;
-                xl[lane + 32][0] = v2.lo;
-            }
-            if (lane == 0) {
-                rh[0] = r.hi;
-                rl[0] = r.lo;
-                if (blockIdx.x == 0) piv[k0] = df_to(v);
-            }
+    // a[x][c] -= sum_t l[x][p0 + t] l[c][p0 + t] over the block's rows x (the pivot block's only
+    // on and below the diagonal) and the columns c0 <= c < c1; work items t0, t0 + nt, ...
+    auto rank_update = [&](int p0, int c0, int c1, int t0, int nt) {
+        const int nc = c1 - c0;
+        for (int e = t0; e < nrow * nc; e += nt) {
+            const int x = e / nc, c = c0 + e % nc;
+            if (x < DNB && x < c) continue;
+            df acc = {0.f, 0.f};
+#pragma unroll
+            for (int t = 0; t < PANEL_SP; ++t)
+                df_fma_lazy(acc, {ph[x][p0 + t], pl[x][p0 + t]}, {ph[c][p0 + t], pl[c][p0 + t]});
+            const df v = df_add({ph[x][c], pl[x][c]}, df_neg(df_norm(acc)));
+            ph[x][c] = v.hi;
+            pl[x][c] = v.lo;
         }
-    }
-    __syncthreads();
-    for (int j = 0; j + 1 < DNB; ++j) {
-        if (bad) break;
-        if (w > j) {
-            const int c = w;
-            const df lc = {ah[c][j], al[c][j]};
-            const bool low = lane >= c;  // pivot row lane, lower triangle
-            df v0 = {0.f, 0.f}, v1 = {0.f, 0.f}, v2 = {0.f, 0.f};
-            if (low) {
-                v0 = {ah[lane][c], al[lane][c]};
-                df_fms_acc(v0, {ah[lane][j], al[lane][j]}, lc);
-            }
-            if (rows) {
-                v1 = {xh[lane][c], xl[lane][c]};
-                df_fms_acc(v1, {xh[lane][j], xl[lane][j]}, lc);
-                v2 = {xh[lane + 32][c], xl[lane + 32][c]};
-                df_fms_acc(v2, {xh[lane + 32][j], xl[lane + 32][j]}, lc);
-            }
-            if (c == j + 1) {
-                const df d = {__shfl_sync(0xffffffffu, v0.hi, c), __shfl_sync(0xffffffffu, v0.lo, c)};
-                if (!(d.hi > 0.f)) {
-                    if (lane == 0) {
-                        bad = 1;
-                        if (blockIdx.x == 0) report(info, AJ_INFO_NOT_POSITIVE_DEFINITE, k0 + c);
+    };
+    __syncthreads();  // the pre-update's writes
+    for (int J = 0; J < DNB / PANEL_SP; ++J) {
+        const int j0 = J * PANEL_SP;
+        if (w < 3) {
+            if (w == 0 || rows) {
+                const int x = w * 32 + lane;
+                df y[PANEL_SP], dv[PANEL_SP];
+#pragma unroll
+                for (int t = 0; t < PANEL_SP; ++t) {
+                    y[t] = {ph[x][j0 + t], pl[x][j0 + t]};
+                    dv[t] = lane < PANEL_SP ? df{ph[j0 + lane][j0 + t], pl[j0 + lane][j0 + t]} : df{0.f, 0.f};
+                }
+                bool ok = true;
+#pragma unroll
+                for (int t = 0; t < PANEL_SP; ++t) {
+                    const int j = j0 + t;
+                    const df d = {__shfl_sync(0xffffffffu, dv[t].hi, t), __shfl_sync(0xffffffffu, dv[t].lo, t)};
+                    if (!(d.hi > 0.f)) {  // the same in every lane and every chain warp
+                        if (w == 0 && lane == 0) {
+                            bad = 1;
+                            if (blockIdx.x == 0) report(info, AJ_INFO_NOT_POSITIVE_DEFINITE, k0 + j);
+                        }
+                        ok = false;
+                        break;
                     }
-                } else {
                     const df r = dfrsqrt(d);
-                    if (low) v0 = lane == c ? dfmul(d, r) : dfmul(v0, r);
-                    if (rows) {
-                        v1 = dfmul(v1, r);
-                        v2 = dfmul(v2, r);
+                    dv[t] = lane == t ? dfmul(d, r) : dfmul(dv[t], r);
+                    y[t] = x == j ? dfmul(d, r) : dfmul(y[t], r);
+                    if (w == 0 && lane == t) {
+                        rh[j] = r.hi;
+                        rl[j] = r.lo;
+                        if (blockIdx.x == 0 && j < nb) piv[k0 + j] = df_to(dv[t]);
                     }
-                    if (lane == c) {
-                        rh[c] = r.hi;
-                        rl[c] = r.lo;
-                        if (blockIdx.x == 0 && c < nb) piv[k0 + c] = df_to(v0);
+#pragma unroll
+                    for (int u = t + 1; u < PANEL_SP; ++u) {
+                        const df lu = {__shfl_sync(0xffffffffu, dv[t].hi, u), __shfl_sync(0xffffffffu, dv[t].lo, u)};
+                        df_fms_acc(dv[u], dv[t], lu);
+                        df_fms_acc(y[u], y[t], lu);
                     }
                 }
+                if (ok)
+#pragma unroll
+                    for (int t = 0; t < PANEL_SP; ++t) {
+                        ph[x][j0 + t] = y[t].hi;
+                        pl[x][j0 + t] = y[t].lo;
+                    }
             }
-            if (low) {
-                ah[lane][c] = v0.hi;
-                al[lane][c] = v0.lo;
-            }
-            if (rows) {
-                xh[lane][c] = v1.hi;
-                xl[lane][c] = v1.lo;
-                xh[lane + 32][c] = v2.hi;
-                xl[lane + 32][c] = v2.lo;
-            }
+        } else if (J > 0) {
+            rank_update(j0 - PANEL_SP, j0 + PANEL_SP, DNB, tid - 96, PANEL_THREADS - 96);
         }
         __syncthreads();
+        if (bad) return;
+        if (J + 1 < DNB / PANEL_SP) {
+            rank_update(j0, j0 + PANEL_SP, j0 + 2 * PANEL_SP, tid, PANEL_THREADS);
+            __syncthreads();
+        }
     }
-    if (bad) return;
     if (blockIdx.x == 0) {
-        // L_kk^-1 by recursive doubling while the other blocks solve and store their rows: at
-        // level b the 32 / (2b) pairs of b x b diagonal blocks (A above C, B the block of L
-        // between them) get their off-diagonal block -C^-1 (B A^-1), through T = B A^-1
+        // the factored pivot block for the final store, and the inverse's diagonal 1 / l_jj for
+        // df_diag_inverse_kernel, which fills in the rest of that block
         for (int e = tid; e < DNB * DNB; e += PANEL_THREADS) {
             const int i = e / DNB, j = e % DNB;
-            ih[i][j] = i == j ? rh[i] : 0.f;
-            il[i][j] = i == j ? rl[i] : 0.f;
-        }
-        __syncthreads();
-        for (int b = 1; b < DNB; b <<= 1) {
-            const int n = (DNB / 2) * b;  // outputs of this level: pairs x b^2
-            const int pair = tid / (b * b), rem = tid % (b * b), r = rem / b, c = rem % b;
-            const int i0 = 2 * b * pair;
-            if (tid < n) {
-                df acc = {0.f, 0.f};
-                for (int q = c; q < b; ++q)
-                    df_fma_acc(acc, {ah[i0 + b + r][i0 + q], al[i0 + b + r][i0 + q]},
-                               {ih[i0 + q][i0 + c], il[i0 + q][i0 + c]});
-                th[tid] = acc.hi;
-                tl[tid] = acc.lo;
+            fh[e] = j <= i ? ph[i][j] : 0.f;
+            fl[e] = j <= i ? pl[i][j] : 0.f;
+            if (i == j) {
+                dh[e] = rh[i];
+                dl[e] = rl[i];
             }
-            __syncthreads();
-            if (tid < n) {
-                df acc = {0.f, 0.f};
-                for (int q = 0; q <= r; ++q)
-                    df_fma_acc(acc, {ih[i0 + b + r][i0 + b + q], il[i0 + b + r][i0 + b + q]},
-                               {th[pair * b * b + q * b + c], tl[pair * b * b + q * b + c]});
-                ih[i0 + b + r][i0 + c] = -acc.hi;
-                il[i0 + b + r][i0 + c] = -acc.lo;
-            }
-            __syncthreads();
-        }
-        float* __restrict__ Ih = z < mats.ninv ? pick(mats.Ih, z) : nullptr;
-        float* __restrict__ Il = z < mats.ninv ? pick(mats.Il, z) : nullptr;
-        for (int e = tid; e < DNB * DNB; e += PANEL_THREADS) {
-            const int i = e / DNB, j = e % DNB;
-            if (Ih && i < nb && j < nb) {
-                const int64_t off = (k0 + i) * S + k0 + j;
-                Ih[off] = ih[i][j];
-                Il[off] = il[i][j];
-            }
-            fh[e] = j <= i ? ah[i][j] : 0.f;
-            fl[e] = j <= i ? al[i][j] : 0.f;
-            dh[e] = ih[i][j];
-            dl[e] = il[i][j];
         }
         return;
     }
@@ -551,9 +510,71 @@ __global__ void __launch_bounds__(PANEL_THREADS)
         const int i = e / DNB, j = e % DNB;
         const int64_t r = r0 + i;
         if (r < S && j < nb) {
-            Lh[r * S + k0 + j] = xh[i][j];
-            Ll[r * S + k0 + j] = xl[i][j];
+            Lh[r * S + k0 + j] = ph[DNB + i][j];
+            Ll[r * S + k0 + j] = pl[DNB + i][j];
         }
+    }
+}
+
+// X = L_kk^-1 of diagonal block kb (the factored block in fh/fl, X's diagonal 1 / l_jj in dh/dl's
+// diagonal) by recursive doubling: at level b the 32 / (2b) pairs of b x b diagonal blocks (A
+// above C, B the block of L between them) get their off-diagonal block -C^-1 (B A^-1), through
+// T = B A^-1.  Writes the whole block to dh/dl and, for a matrix that keeps L^-1, to Ih/Il.
+// One block per matrix (blockIdx.y), on its own lane: only the triangular inverses need it.
+__global__ void __launch_bounds__(256) df_diag_inverse_kernel(DfMats mats, int64_t S, int64_t kb) {
+    const int z = blockIdx.y;
+    const float* __restrict__ fh = pick(mats.fh, z) + kb * DNB * DNB;
+    const float* __restrict__ fl = pick(mats.fl, z) + kb * DNB * DNB;
+    float* __restrict__ dh = pick(mats.dh, z) + kb * DNB * DNB;
+    float* __restrict__ dl = pick(mats.dl, z) + kb * DNB * DNB;
+    __shared__ float lh[DNB][DNB + 1], ll[DNB][DNB + 1];
+    __shared__ float ih[DNB][DNB + 1], il[DNB][DNB + 1];
+    __shared__ float th[DNB * DNB / 4], tl[DNB * DNB / 4];
+    const int tid = threadIdx.x;
+    const int64_t k0 = kb * DNB;
+    const int64_t nb = (S - k0) < DNB ? (S - k0) : DNB;
+    for (int e = tid; e < DNB * DNB; e += blockDim.x) {
+        const int i = e / DNB, j = e % DNB;
+        lh[i][j] = fh[e];
+        ll[i][j] = fl[e];
+        ih[i][j] = i == j ? dh[e] : 0.f;
+        il[i][j] = i == j ? dl[e] : 0.f;
+    }
+    __syncthreads();
+    for (int b = 1; b < DNB; b <<= 1) {
+        const int n = (DNB / 2) * b;  // outputs of this level: pairs x b^2
+        const int pair = tid / (b * b), rem = tid % (b * b), r = rem / b, c = rem % b;
+        const int i0 = 2 * b * pair;
+        if (tid < n) {
+            df acc = {0.f, 0.f};
+            for (int q = c; q < b; ++q)
+                df_fma_acc(acc, {lh[i0 + b + r][i0 + q], ll[i0 + b + r][i0 + q]},
+                           {ih[i0 + q][i0 + c], il[i0 + q][i0 + c]});
+            th[tid] = acc.hi;
+            tl[tid] = acc.lo;
+        }
+        __syncthreads();
+        if (tid < n) {
+            df acc = {0.f, 0.f};
+            for (int q = 0; q <= r; ++q)
+                df_fma_acc(acc, {ih[i0 + b + r][i0 + b + q], il[i0 + b + r][i0 + b + q]},
+                           {th[pair * b * b + q * b + c], tl[pair * b * b + q * b + c]});
+            ih[i0 + b + r][i0 + c] = -acc.hi;
+            il[i0 + b + r][i0 + c] = -acc.lo;
+        }
+        __syncthreads();
+    }
+    float* __restrict__ Ih = z < mats.ninv ? pick(mats.Ih, z) : nullptr;
+    float* __restrict__ Il = z < mats.ninv ? pick(mats.Il, z) : nullptr;
+    for (int e = tid; e < DNB * DNB; e += blockDim.x) {
+        const int i = e / DNB, j = e % DNB;
+        if (Ih && i < nb && j < nb) {
+            const int64_t off = (k0 + i) * S + k0 + j;
+            Ih[off] = ih[i][j];
+            Il[off] = il[i][j];
+        }
+        dh[e] = ih[i][j];
+        dl[e] = il[i][j];
     }
 }
 
@@ -1232,7 +1253,8 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
     Lanes* lanes = nullptr;
     AJ_TRY(lanes_for(st, &lanes));
     Lanes& ln = *lanes;
-    const int nlanes = AIh ? 5 : 2 + n_inverse;  // lanes 2 .. 1 + n_inverse for L^-1, lane 4 for A^-1
+    // lanes 2 .. 1 + n_inverse for L^-1, lane 4 for A^-1, lane 5 for the diagonal blocks' inverses
+    const int nlanes = n_inverse > 0 ? kLaneCount : 2;
     AJ_TRY(lanes_fork(ln, st, nlanes));
     cudaStream_t crit = ln.s[0], bulk = ln.s[1];
     // each matrix's L^-1 on its own lane: a view of m whose slot 0 is matrix z
@@ -1279,8 +1301,12 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
     // Step kb: panel kb + 1 applies panel kb's update to its own block column,
     // so it only has to wait for the bulk update of step kb - 1 (which reached
     // that column); the bulk update of step kb covers the columns after it.
-    cudaStream_t lau = ln.s[4];
+    cudaStream_t lau = ln.s[4], dinv = ln.s[5];
     AJ_TRY(panel(0));
+    if (n_inverse > 0 && nbt == 1) {
+        df_diag_inverse_kernel<<<dim3(1, (unsigned)n_inverse), 256, 0, crit>>>(m, S, 0);
+        AJ_LAUNCHED();
+    }
     if (AIh && nbt == 1) AJ_TRY(lauum_row(0, crit));
     bool rest_prev = false;
     for (int64_t kb = 0; kb + 1 < nbt; ++kb) {
@@ -1303,14 +1329,22 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
         rest_prev = tb > 1;
         AJ_TRY(panel(kb + 1));
         if (n_inverse > 0) {
+            // the diagonal blocks' inverses: block 0 (block row 0 of L^-1) and block kb + 1
+            // (applied by this step's next block row)
             AJ_TRY(lane_signal(ln, kEvDiag, 0));
+            AJ_TRY(lane_wait(ln, 5, kEvDiag));
+            for (int64_t d = kb == 0 ? 0 : kb + 1; d <= kb + 1; ++d) {
+                df_diag_inverse_kernel<<<dim3(1, (unsigned)n_inverse), 256, 0, dinv>>>(m, S, d);
+                AJ_LAUNCHED();
+            }
+            AJ_TRY(lane_signal(ln, kEvInv, 5));
             // rows past the next block row in 64 x 64 tiles when there are enough of them; the
             // next block row (which applies the diagonal inverse) always in 32 x 32 tiles
             const int64_t nI = (S - (kb + 2) * DNB + T64 - 1) / T64, nJ = ((kb + 1) * DNB + T64 - 1) / T64;
             const bool big = nI > 0 && nI * nJ >= g_tile64_min[1];
             const int64_t tiles = (big ? 1 : nbt - kb - 1) * (kb + 1);
             for (int z = 0; z < n_inverse; ++z) {
-                AJ_TRY(lane_wait(ln, 2 + z, kEvDiag));
+                AJ_TRY(lane_wait(ln, 2 + z, kEvInv));
                 df_trtri_step_kernel<<<(unsigned)tiles, 256, 0, ln.s[2 + z]>>>(one[z], S, kb);
                 AJ_LAUNCHED();
                 if (big) {
