@@ -38,16 +38,14 @@ int spd_inverse_from_factor(int64_t S, SpdWorkspace& w, double* Ainv, cudaStream
 // ---- lanes.cu (side streams that fork from and join back into the caller's stream)
 
 // 0: critical chain (highest priority), 1: bulk updates, 2: triangular inverse
-// of the first matrix, 3: triangular inverse of the second, 4: A^-1 of the first,
-// 5: the inverses of the diagonal blocks
-constexpr int kLaneCount = 6;
+// of the first matrix, 3: triangular inverse of the second, 4: A^-1 of the first
+constexpr int kLaneCount = 5;
 enum LaneEvent {
     kEvFork = 0,
     kEvPanel,
     kEvUpdate,
     kEvDiag,
     kEvRow,      // a block row of the first matrix's L^-1 is final
-    kEvInv,      // a diagonal block's inverse is final
     kEvPre,      // the evaluation's independent pre-work forks here ...
     kEvPreDone,  // ... and is joined here
     kEvJoin0,

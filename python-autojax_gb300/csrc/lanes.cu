@@ -4,9 +4,8 @@
 // run faster as concurrent chains: the critical one (the pivot panels) on a
 // high-priority stream, the bulk of each trailing update on a low-priority
 // one, the triangular inverses, which need only finished panels, on a third
-// and a fourth (one per matrix), A^-1 = L^-T L^-1, which needs only
-// finished rows of L^-1, on a fifth, and the inverses of the diagonal blocks,
-// which the triangular inverses apply, on a sixth.  Every fork starts
+// and a fourth (one per matrix), and A^-1 = L^-T L^-1, which needs only
+// finished rows of L^-1, on a fifth.  Every fork starts
 // with an event recorded on the caller's stream and every join ends with the
 // caller's stream waiting on each lane, so the caller sees one ordered stream,
 // and stream capture records the same dependencies as graph edges.
@@ -33,7 +32,7 @@ int create_lanes(Lanes& l) {
     int least = 0, greatest = 0;
     if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return AJ_ERR_CUDA;
     const int mid = greatest < least ? greatest + 1 : least;
-    const int prio[kLaneCount] = {greatest, least, mid, mid, mid, mid};
+    const int prio[kLaneCount] = {greatest, least, mid, mid, mid};
     for (int i = 0; i < kLaneCount; ++i)
         if (cudaStreamCreateWithPriority(&l.s[i], cudaStreamNonBlocking, prio[i]) != cudaSuccess) return AJ_ERR_CUDA;
     for (int i = 0; i < kLaneEvents; ++i)

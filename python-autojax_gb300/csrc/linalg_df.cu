@@ -34,7 +34,7 @@ struct DfMats {
     float* fh[2];  // factored diagonal blocks (copied into L after the last panel)
     float* fl[2];
     double* piv[2];
-    int ninv;  // matrices z < ninv also get L^-1: df_diag_inverse_kernel writes its diagonal blocks
+    int ninv;  // matrices z < ninv also get L^-1: the panel writes its diagonal block
 };
 
 // element z of a kernel-parameter pair without indexing it dynamically (which
@@ -289,9 +289,8 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 // b >= 1, solve the 64 panel rows k0 + 32 + 64 (b - 1) .. for L's columns
 // (rows <- A_rows L_kk^-T) in the same column loop.  Block 0 stores L_kk (in
 // the factored-block buffer, not in L: blocks of the same launch may start
-// late and must still read the unfactored block from L), the pivots and the
-// inverse's diagonal 1 / l_jj; df_diag_inverse_kernel completes L_kk^-1 on a
-// lane of its own, off the critical chain.
+// late and must still read the unfactored block from L), the pivots and
+// L_kk^-1, which it computes while the other blocks store their rows.
 // Latency matters more than work here (one launch per 32 columns sits on the
 // critical path), so the column loop takes one barrier a column and lets each
 // finished column's warp drop out.
@@ -493,16 +492,55 @@ __global__ void __launch_bounds__(PANEL_THREADS)
         }
     }
     if (blockIdx.x == 0) {
-        // the factored pivot block for the final store, and the inverse's diagonal 1 / l_jj for
-        // df_diag_inverse_kernel, which fills in the rest of that block
+        // L_kk^-1 by recursive doubling while the other blocks store their rows: at level b the
+        // 32 / (2b) pairs of b x b diagonal blocks (A above C, B the block of L between them) get
+        // their off-diagonal block -C^-1 (B A^-1), through T = B A^-1
+        float(*ih)[DNB + 1] = ph + DNB;  // the block has no panel rows: their space holds L_kk^-1
+        float(*il)[DNB + 1] = pl + DNB;
+        float* th = &ph[2 * DNB][0];
+        float* tl = &pl[2 * DNB][0];
         for (int e = tid; e < DNB * DNB; e += PANEL_THREADS) {
             const int i = e / DNB, j = e % DNB;
+            ih[i][j] = i == j ? rh[i] : 0.f;
+            il[i][j] = i == j ? rl[i] : 0.f;
+        }
+        __syncthreads();
+        for (int b = 1; b < DNB; b <<= 1) {
+            const int n = (DNB / 2) * b;  // outputs of this level: pairs x b^2
+            const int pair = tid / (b * b), rem = tid % (b * b), r = rem / b, c = rem % b;
+            const int i0 = 2 * b * pair;
+            if (tid < n) {
+                df acc = {0.f, 0.f};
+                for (int q = c; q < b; ++q)
+                    df_fma_acc(acc, {ph[i0 + b + r][i0 + q], pl[i0 + b + r][i0 + q]},
+                               {ih[i0 + q][i0 + c], il[i0 + q][i0 + c]});
+                th[tid] = acc.hi;
+                tl[tid] = acc.lo;
+            }
+            __syncthreads();
+            if (tid < n) {
+                df acc = {0.f, 0.f};
+                for (int q = 0; q <= r; ++q)
+                    df_fma_acc(acc, {ih[i0 + b + r][i0 + b + q], il[i0 + b + r][i0 + b + q]},
+                               {th[pair * b * b + q * b + c], tl[pair * b * b + q * b + c]});
+                ih[i0 + b + r][i0 + c] = -acc.hi;
+                il[i0 + b + r][i0 + c] = -acc.lo;
+            }
+            __syncthreads();
+        }
+        float* __restrict__ Ih = z < mats.ninv ? pick(mats.Ih, z) : nullptr;
+        float* __restrict__ Il = z < mats.ninv ? pick(mats.Il, z) : nullptr;
+        for (int e = tid; e < DNB * DNB; e += PANEL_THREADS) {
+            const int i = e / DNB, j = e % DNB;
+            if (Ih && i < nb && j < nb) {
+                const int64_t off = (k0 + i) * S + k0 + j;
+                Ih[off] = ih[i][j];
+                Il[off] = il[i][j];
+            }
             fh[e] = j <= i ? ph[i][j] : 0.f;
             fl[e] = j <= i ? pl[i][j] : 0.f;
-            if (i == j) {
-                dh[e] = rh[i];
-                dl[e] = rl[i];
-            }
+            dh[e] = ih[i][j];
+            dl[e] = il[i][j];
         }
         return;
     }
@@ -513,68 +551,6 @@ __global__ void __launch_bounds__(PANEL_THREADS)
             Lh[r * S + k0 + j] = ph[DNB + i][j];
             Ll[r * S + k0 + j] = pl[DNB + i][j];
         }
-    }
-}
-
-// X = L_kk^-1 of diagonal block kb (the factored block in fh/fl, X's diagonal 1 / l_jj in dh/dl's
-// diagonal) by recursive doubling: at level b the 32 / (2b) pairs of b x b diagonal blocks (A
-// above C, B the block of L between them) get their off-diagonal block -C^-1 (B A^-1), through
-// T = B A^-1.  Writes the whole block to dh/dl and, for a matrix that keeps L^-1, to Ih/Il.
-// One block per matrix (blockIdx.y), on its own lane: only the triangular inverses need it.
-__global__ void __launch_bounds__(256) df_diag_inverse_kernel(DfMats mats, int64_t S, int64_t kb) {
-    const int z = blockIdx.y;
-    const float* __restrict__ fh = pick(mats.fh, z) + kb * DNB * DNB;
-    const float* __restrict__ fl = pick(mats.fl, z) + kb * DNB * DNB;
-    float* __restrict__ dh = pick(mats.dh, z) + kb * DNB * DNB;
-    float* __restrict__ dl = pick(mats.dl, z) + kb * DNB * DNB;
-    __shared__ float lh[DNB][DNB + 1], ll[DNB][DNB + 1];
-    __shared__ float ih[DNB][DNB + 1], il[DNB][DNB + 1];
-    __shared__ float th[DNB * DNB / 4], tl[DNB * DNB / 4];
-    const int tid = threadIdx.x;
-    const int64_t k0 = kb * DNB;
-    const int64_t nb = (S - k0) < DNB ? (S - k0) : DNB;
-    for (int e = tid; e < DNB * DNB; e += blockDim.x) {
-        const int i = e / DNB, j = e % DNB;
-        lh[i][j] = fh[e];
-        ll[i][j] = fl[e];
-        ih[i][j] = i == j ? dh[e] : 0.f;
-        il[i][j] = i == j ? dl[e] : 0.f;
-    }
-    __syncthreads();
-    for (int b = 1; b < DNB; b <<= 1) {
-        const int n = (DNB / 2) * b;  // outputs of this level: pairs x b^2
-        const int pair = tid / (b * b), rem = tid % (b * b), r = rem / b, c = rem % b;
-        const int i0 = 2 * b * pair;
-        if (tid < n) {
-            df acc = {0.f, 0.f};
-            for (int q = c; q < b; ++q)
-                df_fma_acc(acc, {lh[i0 + b + r][i0 + q], ll[i0 + b + r][i0 + q]},
-                           {ih[i0 + q][i0 + c], il[i0 + q][i0 + c]});
-            th[tid] = acc.hi;
-            tl[tid] = acc.lo;
-        }
-        __syncthreads();
-        if (tid < n) {
-            df acc = {0.f, 0.f};
-            for (int q = 0; q <= r; ++q)
-                df_fma_acc(acc, {ih[i0 + b + r][i0 + b + q], il[i0 + b + r][i0 + b + q]},
-                           {th[pair * b * b + q * b + c], tl[pair * b * b + q * b + c]});
-            ih[i0 + b + r][i0 + c] = -acc.hi;
-            il[i0 + b + r][i0 + c] = -acc.lo;
-        }
-        __syncthreads();
-    }
-    float* __restrict__ Ih = z < mats.ninv ? pick(mats.Ih, z) : nullptr;
-    float* __restrict__ Il = z < mats.ninv ? pick(mats.Il, z) : nullptr;
-    for (int e = tid; e < DNB * DNB; e += blockDim.x) {
-        const int i = e / DNB, j = e % DNB;
-        if (Ih && i < nb && j < nb) {
-            const int64_t off = (k0 + i) * S + k0 + j;
-            Ih[off] = ih[i][j];
-            Il[off] = il[i][j];
-        }
-        dh[e] = ih[i][j];
-        dl[e] = il[i][j];
     }
 }
 
@@ -1253,8 +1229,7 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
     Lanes* lanes = nullptr;
     AJ_TRY(lanes_for(st, &lanes));
     Lanes& ln = *lanes;
-    // lanes 2 .. 1 + n_inverse for L^-1, lane 4 for A^-1, lane 5 for the diagonal blocks' inverses
-    const int nlanes = n_inverse > 0 ? kLaneCount : 2;
+    const int nlanes = AIh ? 5 : 2 + n_inverse;  // lanes 2 .. 1 + n_inverse for L^-1, lane 4 for A^-1
     AJ_TRY(lanes_fork(ln, st, nlanes));
     cudaStream_t crit = ln.s[0], bulk = ln.s[1];
     // each matrix's L^-1 on its own lane: a view of m whose slot 0 is matrix z
@@ -1301,12 +1276,8 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
     // Step kb: panel kb + 1 applies panel kb's update to its own block column,
     // so it only has to wait for the bulk update of step kb - 1 (which reached
     // that column); the bulk update of step kb covers the columns after it.
-    cudaStream_t lau = ln.s[4], dinv = ln.s[5];
+    cudaStream_t lau = ln.s[4];
     AJ_TRY(panel(0));
-    if (n_inverse > 0 && nbt == 1) {
-        df_diag_inverse_kernel<<<dim3(1, (unsigned)n_inverse), 256, 0, crit>>>(m, S, 0);
-        AJ_LAUNCHED();
-    }
     if (AIh && nbt == 1) AJ_TRY(lauum_row(0, crit));
     bool rest_prev = false;
     for (int64_t kb = 0; kb + 1 < nbt; ++kb) {
@@ -1329,22 +1300,14 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
         rest_prev = tb > 1;
         AJ_TRY(panel(kb + 1));
         if (n_inverse > 0) {
-            // the diagonal blocks' inverses: block 0 (block row 0 of L^-1) and block kb + 1
-            // (applied by this step's next block row)
             AJ_TRY(lane_signal(ln, kEvDiag, 0));
-            AJ_TRY(lane_wait(ln, 5, kEvDiag));
-            for (int64_t d = kb == 0 ? 0 : kb + 1; d <= kb + 1; ++d) {
-                df_diag_inverse_kernel<<<dim3(1, (unsigned)n_inverse), 256, 0, dinv>>>(m, S, d);
-                AJ_LAUNCHED();
-            }
-            AJ_TRY(lane_signal(ln, kEvInv, 5));
             // rows past the next block row in 64 x 64 tiles when there are enough of them; the
             // next block row (which applies the diagonal inverse) always in 32 x 32 tiles
             const int64_t nI = (S - (kb + 2) * DNB + T64 - 1) / T64, nJ = ((kb + 1) * DNB + T64 - 1) / T64;
             const bool big = nI > 0 && nI * nJ >= g_tile64_min[1];
             const int64_t tiles = (big ? 1 : nbt - kb - 1) * (kb + 1);
             for (int z = 0; z < n_inverse; ++z) {
-                AJ_TRY(lane_wait(ln, 2 + z, kEvInv));
+                AJ_TRY(lane_wait(ln, 2 + z, kEvDiag));
                 df_trtri_step_kernel<<<(unsigned)tiles, 256, 0, ln.s[2 + z]>>>(one[z], S, kb);
                 AJ_LAUNCHED();
                 if (big) {
