@@ -82,6 +82,9 @@ int df_split(const double* x, int64_t n, float* hi, float* lo, cudaStream_t st);
 int df_mirror_lower(float* hi, float* lo, int64_t S, cudaStream_t st);
 int df_join(const float* hi, const float* lo, int64_t n, double* x, cudaStream_t st);
 int df_add_f64(const float* ah, const float* al, const double* b, int64_t n, float* oh, float* ol, cudaStream_t st);
+// o = a + b (S x S planes + float64) and its lower triangle, upper zero, in lo_h/lo_l
+int df_add_f64_lower(const float* ah, const float* al, const double* b, int64_t S, float* oh, float* ol, float* lo_h,
+                     float* lo_l, cudaStream_t st);
 int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const float* Ah, const float* Al, int64_t lda,
             const float* Bh, const float* Bl, int64_t ldb, bool accumulate, float* Ch, float* Cl, int64_t ldc,
             bool lower_only, bool tri_k, cudaStream_t st);
@@ -93,7 +96,7 @@ int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* 
 // up the same way, one finished block row of L^-1 at a time.
 int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int count, int n_inverse, int64_t S,
                           DfSpd* const* w, double* const* logdet, int* info, cudaStream_t st, float* AIh = nullptr,
-                          float* AIl = nullptr);
+                          float* AIl = nullptr, bool prepared = false);
 // x = A^-1 b through the inverse factor (two triangular products)
 int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st);
 int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x, double* r,
@@ -128,6 +131,10 @@ int csc_spmm_t(const Csc& c, int64_t S, const Tin* X, int64_t ld_x, int64_t cols
 // double-float planes: out (S x cols) = T^T X with X given as (hi, lo) planes
 int csc_spmm_t_df(const Csc& c, int64_t S, const float* Xh, const float* Xl, int64_t ld_x, int64_t cols, float* Oh,
                   float* Ol, int64_t ld_out, cudaStream_t st);
+// the same with the output transposed: out (cols x S, leading dimension ld_out) = (T^T X)^T, bit-identical
+// to transposing csc_spmm_t_df's output; needs X rows 16-byte aligned and cols % 4 == 0
+int csc_spmm_t_df_tr(const Csc& c, int64_t S, const float* Xh, const float* Xl, int64_t ld_x, int64_t cols, float* Oh,
+                     float* Ol, int64_t ld_out, cudaStream_t st);
 // out[s] = sum_e val[e] * x[row[e]]
 int csc_spmv_t(const Csc& c, int64_t S, const double* x, double* out, cudaStream_t st);
 // TW (S x M) with TW[s][m1] = sum_e val[e] * Wc(m1, row[e]) from the compact table (T float or double)

@@ -283,7 +283,7 @@ __global__ void split_shifted_kernel(const double* __restrict__ H, int64_t S, co
     const double add = shift[0] / (double)S;
     const int64_t n = S * S;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-        const df v = df_from(H[t] + add);
+        const df v = t % S <= t / S ? df_from(H[t] + add) : df{0.f, 0.f};  // lower triangle only
         hi[t] = v.hi;
         lo[t] = v.lo;
     }
@@ -316,7 +316,7 @@ struct EvidenceBufs {
     DfSpd da{}, dh{};                 // mixed path
     double *TW, *Om, *F, *H, *A, *Ainv, *D, *s, *res, *kpart, *fpart, *logdets;
     float *Wh, *Wl;                   // w_tilde planes when split per call
-    float *TWh, *TWl, *Omh, *Oml, *Fh, *Fl, *Hh, *Hl, *Ah, *Al, *AIh, *AIl, *sh, *sl;
+    float *TWh, *TWl, *Omh, *Oml, *Fh, *Fl, *Ah, *Al, *AIh, *AIl, *sh, *sl;
     int64_t nk_blocks, nfrob;
     bool compact, grad, mixed;
 };
@@ -372,15 +372,15 @@ size_t evidence_carve(const aj_problem* p, bool mixed, bool with_grad, void* bas
             b.Wh = cv.take<float>(M * M);
             b.Wl = cv.take<float>(M * M);
         }
-        if (b.compact) b.TW = cv.take<double>(S * M);
-        b.TWh = cv.take<float>(S * M);
-        b.TWl = cv.take<float>(S * M);
+        if (b.compact) {
+            b.TW = cv.take<double>(S * M);
+            b.TWh = cv.take<float>(S * M);
+            b.TWl = cv.take<float>(S * M);
+        }
         b.Omh = cv.take<float>(M * S);
         b.Oml = cv.take<float>(M * S);
         b.Fh = cv.take<float>(S * S);
         b.Fl = cv.take<float>(S * S);
-        b.Hh = cv.take<float>(S * S);
-        b.Hl = cv.take<float>(S * S);
         b.Ah = cv.take<float>(S * S);
         b.Al = cv.take<float>(S * S);
         {
@@ -474,9 +474,17 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
                                                          p->coefficient_dev, b.logdets + 4);
             rc = check_launch();
             if (rc == AJ_OK) {
+                // straight into H's factorisation workspace, and the inverse buffers zeroed here too,
+                // so the factorisation starts without copies
                 split_shifted_kernel<<<blocks_for(S * S, 256, 8 * num_sms()), 256, 0, pre>>>(b.H, S, b.logdets + 4,
-                                                                                             b.Hh, b.Hl);
+                                                                                             b.dh.Lh, b.dh.Ll);
                 rc = check_launch();
+                if (rc == AJ_OK &&
+                    (cudaMemsetAsync(b.da.Ih, 0, sizeof(float) * 2 * S * S, pre) != cudaSuccess ||
+                     (with_grad && (cudaMemsetAsync(b.dh.Ih, 0, sizeof(float) * 2 * S * S, pre) != cudaSuccess ||
+                                    cudaMemsetAsync(b.AIh, 0, sizeof(float) * S * S, pre) != cudaSuccess ||
+                                    cudaMemsetAsync(b.AIl, 0, sizeof(float) * S * S, pre) != cudaSuccess))))
+                    rc = AJ_ERR_CUDA;
             }
         }
         if (rc == AJ_OK) {
@@ -524,20 +532,24 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
                 Wh = b.Wh;
                 Wl = b.Wl;
             }
-            AJ_TRY(csc_spmm_t_df(b.cs, S, Wh, Wl, M, M, b.TWh, b.TWl, M, st));
+            // Omega = (T^T W)^T straight from the gather
+            AJ_TRY(csc_spmm_t_df_tr(b.cs, S, Wh, Wl, M, M, b.Omh, b.Oml, S, st));
         }
-        AJ_TRY(transpose<float>(b.TWh, S, M, b.Omh, st));
-        AJ_TRY(transpose<float>(b.TWl, S, M, b.Oml, st));
+        if (b.compact) {
+            AJ_TRY(transpose<float>(b.TWh, S, M, b.Omh, st));
+            AJ_TRY(transpose<float>(b.TWl, S, M, b.Oml, st));
+        }
         AJ_TRY(csc_spmm_t_df(b.cs, S, b.Omh, b.Oml, S, S, b.Fh, b.Fl, S, st));
         AJ_TRY(join_pre());
-        AJ_TRY(df_add_f64(b.Fh, b.Fl, b.H, S * S, b.Ah, b.Al, st));
+        // A (in full for the refinement's residual) and its lower triangle for the factorisation
+        AJ_TRY(df_add_f64_lower(b.Fh, b.Fl, b.H, S, b.Ah, b.Al, b.da.Lh, b.da.Ll, st));
         // A and H share every factorisation launch (and, with the gradient, every inversion launch)
-        const float* fh[2] = {b.Ah, b.Hh};
-        const float* fl[2] = {b.Al, b.Hl};
+        const float* fh[2] = {b.da.Lh, b.dh.Lh};
+        const float* fl[2] = {b.da.Ll, b.dh.Ll};
         DfSpd* fw[2] = {&b.da, &b.dh};
         double* ld[2] = {b.logdets + 0, b.logdets + 1};
         AJ_TRY(dfspd_factor_invert_n(fh, fl, 2, with_grad ? 2 : 1, S, fw, ld, info, st, with_grad ? b.AIh : nullptr,
-                                     with_grad ? b.AIl : nullptr));
+                                     with_grad ? b.AIl : nullptr, true));
         AJ_TRY(dfspd_solve_refined(S, b.da, b.Ah, b.Al, b.D, b.s, b.res, st, with_grad ? b.AIh : nullptr,
                                    with_grad ? b.AIl : nullptr));
     }

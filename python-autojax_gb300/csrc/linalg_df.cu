@@ -1168,6 +1168,28 @@ int df_add_f64(const float* ah, const float* al, const double* b, int64_t n, flo
     return check_launch();
 }
 
+// o = a + b (S x S) and, in the same pass, its lower triangle with a zero upper triangle in lo_h/lo_l
+// (a factorisation's starting copy)
+__global__ void add_df_f64_lower_kernel(const float* __restrict__ ah, const float* __restrict__ al,
+                                        const double* __restrict__ b, int64_t S, float* __restrict__ oh,
+                                        float* __restrict__ ol, float* __restrict__ lo_h, float* __restrict__ lo_l) {
+    const int64_t n = S * S;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const df v = df_add({ah[t], al[t]}, df_from(b[t]));
+        oh[t] = v.hi;
+        ol[t] = v.lo;
+        const bool low = t % S <= t / S;
+        lo_h[t] = low ? v.hi : 0.f;
+        lo_l[t] = low ? v.lo : 0.f;
+    }
+}
+
+int df_add_f64_lower(const float* ah, const float* al, const double* b, int64_t S, float* oh, float* ol, float* lo_h,
+                     float* lo_l, cudaStream_t st) {
+    add_df_f64_lower_kernel<<<blocks_for(S * S, 256, 8 * num_sms()), 256, 0, st>>>(ah, al, b, S, oh, ol, lo_h, lo_l);
+    return check_launch();
+}
+
 static DfMats mats_of(DfSpd* const* w, int count) {
     DfMats m{};
     for (int z = 0; z < 2; ++z) {
@@ -1191,7 +1213,8 @@ static DfMats mats_of(DfSpd* const* w, int count) {
 static int g_tile64_min[3] = {128, 128, 96};  // trailing update, L^-1 step, A^-1 row
 
 // L (in w[z]) = chol(A[z]) for z < count (1 or 2), and L^-1 for z < n_inverse; A given as planes
-// (copied unless it is w's own L).
+// (copied unless it is w's own L).  With `prepared` the caller has already put each A's lower
+// triangle, upper triangle zero, in w[z]'s L and zeroed the L^-1 and A^-1 buffers.
 //
 // Three lanes forked from st (lanes.cu).  Lane 0 carries the critical chain:
 // the pivot panel of step k, then the update of block column k + 1 alone, so
@@ -1202,12 +1225,12 @@ static int g_tile64_min[3] = {128, 128, 96};  // trailing update, L^-1 step, A^-
 // is done, so it trails the factorisation by one panel.
 int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int count, int n_inverse, int64_t S,
                           DfSpd* const* w, double* const* logdet, int* info, cudaStream_t st, float* AIh,
-                          float* AIl) {
+                          float* AIl, bool prepared) {
     if (S <= 0) return AJ_OK;
     if (count < 1 || count > 2 || n_inverse < 0 || n_inverse > count) return AJ_ERR_ARG;
     if ((AIh || AIl) && (!AIh || !AIl || n_inverse < 1)) return AJ_ERR_ARG;
     dim3 zg(blocks_for(S, 256, 8), (unsigned)(S < 65535 ? S : 65535));
-    for (int z = 0; z < count; ++z) {
+    for (int z = 0; z < count && !prepared; ++z) {
         if (Ah[z] != w[z]->Lh) {
             if (cudaMemcpyAsync(w[z]->Lh, Ah[z], sizeof(float) * S * S, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
                 cudaMemcpyAsync(w[z]->Ll, Al[z], sizeof(float) * S * S, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
@@ -1219,10 +1242,12 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
     }
     for (int z = 0; z < n_inverse; ++z) {
         if (!w[z]->Ih) return AJ_ERR_ARG;
-        if (cudaMemsetAsync(w[z]->Ih, 0, sizeof(float) * 2 * S * S, st) != cudaSuccess) return AJ_ERR_CUDA;
+        if (!prepared && cudaMemsetAsync(w[z]->Ih, 0, sizeof(float) * 2 * S * S, st) != cudaSuccess)
+            return AJ_ERR_CUDA;
     }
-    if (AIh && (cudaMemsetAsync(AIh, 0, sizeof(float) * S * S, st) != cudaSuccess ||
-                cudaMemsetAsync(AIl, 0, sizeof(float) * S * S, st) != cudaSuccess))
+    if (AIh && !prepared &&
+        (cudaMemsetAsync(AIh, 0, sizeof(float) * S * S, st) != cudaSuccess ||
+         cudaMemsetAsync(AIl, 0, sizeof(float) * S * S, st) != cudaSuccess))
         return AJ_ERR_CUDA;
     DfMats m = mats_of(w, count);
     m.ninv = n_inverse;

@@ -356,6 +356,101 @@ __global__ void __launch_bounds__(256)
     *reinterpret_cast<float4*>(Ol + s * ld_out + c0) = make_float4(acc[0].lo, acc[1].lo, acc[2].lo, acc[3].lo);
 }
 
+// The same gather with the output transposed (out[c][s], e.g. Omega = (T^T W)^T): a block takes
+// 8 source pixels over one 512-column chunk, one pixel after another with the entry order, the
+// grouping and the renormalisation of csc_spmm_t_df_vec_kernel (so each sum is bit-identical),
+// keeps the results in shared memory and stores 8 consecutive pixels (32 bytes) per output row.
+constexpr int kTrPix = 8;
+constexpr int kTrCols = 512;
+
+__global__ void __launch_bounds__(128)
+    csc_spmm_t_df_tr_kernel(const int* __restrict__ colptr, const int* __restrict__ rows,
+                            const float2* __restrict__ vdf, const float* __restrict__ Xh,
+                            const float* __restrict__ Xl, int64_t ld_x, int64_t cols, int64_t S,
+                            float* __restrict__ Oh, float* __restrict__ Ol, int64_t ld_out) {
+    __shared__ int srow[kGatherStage];
+    __shared__ float2 sw[kGatherStage];
+    __shared__ float th[kTrPix][kTrCols], tl[kTrPix][kTrCols];
+    const int64_t s0 = (int64_t)blockIdx.x * kTrPix;
+    const int64_t cbase = (int64_t)blockIdx.y * kTrCols;
+    const int cl = threadIdx.x * 4;
+    const int64_t c0 = cbase + cl;
+    const bool live = c0 < cols;
+    for (int sp = 0; sp < kTrPix; ++sp) {
+        const int64_t s = s0 + sp;
+        if (s >= S) break;
+        df acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        const int b = colptr[s], e = colptr[s + 1];
+        int group = 0;
+        for (int seg = b; seg < e; seg += kGatherStage) {
+            const int n = min(kGatherStage, e - seg);
+            __syncthreads();  // the previous pass's reads of the staged entries are done
+            for (int t = threadIdx.x; t < n; t += blockDim.x) {
+                srow[t] = rows[seg + t];
+                sw[t] = vdf[seg + t];
+            }
+            __syncthreads();
+            if (!live) continue;
+            float4 h[4], l[4];
+            float2 a[4];
+            gather_group(srow, sw, Xh, Xl, ld_x, c0, 0, n, h, l, a);
+            for (int q = 0; q < n; q += 4) {
+                float4 hn[4], ln[4];
+                float2 an[4];
+                const bool more = q + 4 < n;
+                if (more) gather_group(srow, sw, Xh, Xl, ld_x, c0, q + 4, n, hn, ln, an);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const df w = {a[u].x, a[u].y};
+                    df_fma_lazy(acc[0], w, {h[u].x, l[u].x});
+                    df_fma_lazy(acc[1], w, {h[u].y, l[u].y});
+                    df_fma_lazy(acc[2], w, {h[u].z, l[u].z});
+                    df_fma_lazy(acc[3], w, {h[u].w, l[u].w});
+                }
+                if (++group % 2 == 0)
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) df_renorm(acc[v]);
+                if (more) {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        h[u] = hn[u];
+                        l[u] = ln[u];
+                        a[u] = an[u];
+                    }
+                }
+            }
+        }
+        if (live) {
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                df_renorm(acc[v]);
+                th[sp][cl + v] = acc[v].hi;
+                tl[sp][cl + v] = acc[v].lo;
+            }
+        }
+    }
+    __syncthreads();
+    const int np = (int)(S - s0 < kTrPix ? S - s0 : kTrPix);
+    const bool vec = np == kTrPix && ld_out % 4 == 0 && s0 % 4 == 0;
+    for (int r = threadIdx.x; r < kTrCols; r += blockDim.x) {
+        const int64_t c = cbase + r;
+        if (c >= cols) break;
+        float* oh = Oh + c * ld_out + s0;
+        float* ol = Ol + c * ld_out + s0;
+        if (vec) {
+            reinterpret_cast<float4*>(oh)[0] = make_float4(th[0][r], th[1][r], th[2][r], th[3][r]);
+            reinterpret_cast<float4*>(oh)[1] = make_float4(th[4][r], th[5][r], th[6][r], th[7][r]);
+            reinterpret_cast<float4*>(ol)[0] = make_float4(tl[0][r], tl[1][r], tl[2][r], tl[3][r]);
+            reinterpret_cast<float4*>(ol)[1] = make_float4(tl[4][r], tl[5][r], tl[6][r], tl[7][r]);
+        } else {
+            for (int sp = 0; sp < np; ++sp) {
+                oh[sp] = th[sp][r];
+                ol[sp] = tl[sp][r];
+            }
+        }
+    }
+}
+
 __global__ void csc_spmv_t_kernel(const int* __restrict__ colptr, const int* __restrict__ rows,
                                   const double* __restrict__ vals, int64_t S, const double* __restrict__ x,
                                   double* __restrict__ out) {
@@ -553,6 +648,19 @@ int csc_spmm_t_df(const Csc& c, int64_t S, const float* Xh, const float* Xl, int
         csc_spmm_t_df_vec_kernel<<<grid, 128, 0, st>>>(c.colptr, c.rows, c.vdf, Xh, Xl, ld_x, cols, Oh, Ol, ld_out);
     else
         csc_spmm_t_df_kernel<<<grid, 128, 0, st>>>(c.colptr, c.rows, c.vdf, Xh, Xl, ld_x, cols, Oh, Ol, ld_out);
+    return check_launch();
+}
+
+int csc_spmm_t_df_tr(const Csc& c, int64_t S, const float* Xh, const float* Xl, int64_t ld_x, int64_t cols, float* Oh,
+                     float* Ol, int64_t ld_out, cudaStream_t st) {
+    if (S == 0 || cols == 0) return AJ_OK;
+    const bool vec = (cols % 4 == 0) && (ld_x % 4 == 0) && (reinterpret_cast<uintptr_t>(Xh) % 16 == 0) &&
+                     (reinterpret_cast<uintptr_t>(Xl) % 16 == 0) && (reinterpret_cast<uintptr_t>(Oh) % 16 == 0) &&
+                     (reinterpret_cast<uintptr_t>(Ol) % 16 == 0);
+    if (!vec) return AJ_ERR_ARG;
+    dim3 grid((unsigned)((S + kTrPix - 1) / kTrPix), (unsigned)((cols + kTrCols - 1) / kTrCols));
+    csc_spmm_t_df_tr_kernel<<<grid, kTrCols / 4, 0, st>>>(c.colptr, c.rows, c.vdf, Xh, Xl, ld_x, cols, S, Oh, Ol,
+                                                           ld_out);
     return check_launch();
 }
 
