@@ -82,9 +82,10 @@ int df_split(const double* x, int64_t n, float* hi, float* lo, cudaStream_t st);
 int df_mirror_lower(float* hi, float* lo, int64_t S, cudaStream_t st);
 int df_join(const float* hi, const float* lo, int64_t n, double* x, cudaStream_t st);
 int df_add_f64(const float* ah, const float* al, const double* b, int64_t n, float* oh, float* ol, cudaStream_t st);
-// o = a + b (S x S planes + float64) and its lower triangle, upper zero, in lo_h/lo_l
-int df_add_f64_lower(const float* ah, const float* al, const double* b, int64_t S, float* oh, float* ol, float* lo_h,
-                     float* lo_l, cudaStream_t st);
+// A = F + H (S x S) from F's lower triangle (F planes, H float64): A symmetric in full, and its
+// lower triangle, upper zero, in lo_h/lo_l
+int df_add_f64_sym(const float* fh, const float* fl, const double* h, int64_t S, float* ah, float* al, float* lo_h,
+                   float* lo_l, cudaStream_t st);
 int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const float* Ah, const float* Al, int64_t lda,
             const float* Bh, const float* Bl, int64_t ldb, bool accumulate, float* Ch, float* Cl, int64_t ldc,
             bool lower_only, bool tri_k, cudaStream_t st);
@@ -129,8 +130,9 @@ template <typename Tin, typename Tout>
 int csc_spmm_t(const Csc& c, int64_t S, const Tin* X, int64_t ld_x, int64_t cols, Tout* out, int64_t ld_out,
                cudaStream_t st);
 // double-float planes: out (S x cols) = T^T X with X given as (hi, lo) planes
+// (lower: only out[s][c] with c <= s is written)
 int csc_spmm_t_df(const Csc& c, int64_t S, const float* Xh, const float* Xl, int64_t ld_x, int64_t cols, float* Oh,
-                  float* Ol, int64_t ld_out, cudaStream_t st);
+                  float* Ol, int64_t ld_out, cudaStream_t st, bool lower = false);
 // the same with the output transposed: out (cols x S, leading dimension ld_out) = (T^T X)^T, bit-identical
 // to transposing csc_spmm_t_df's output; needs X rows 16-byte aligned and cols % 4 == 0
 int csc_spmm_t_df_tr(const Csc& c, int64_t S, const float* Xh, const float* Xl, int64_t ld_x, int64_t cols, float* Oh,

@@ -539,10 +539,11 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
             AJ_TRY(transpose<float>(b.TWh, S, M, b.Omh, st));
             AJ_TRY(transpose<float>(b.TWl, S, M, b.Oml, st));
         }
-        AJ_TRY(csc_spmm_t_df(b.cs, S, b.Omh, b.Oml, S, S, b.Fh, b.Fl, S, st));
+        // F's lower triangle (F is symmetric); A in full for the refinement's residual and its
+        // lower triangle for the factorisation
+        AJ_TRY(csc_spmm_t_df(b.cs, S, b.Omh, b.Oml, S, S, b.Fh, b.Fl, S, st, true));
         AJ_TRY(join_pre());
-        // A (in full for the refinement's residual) and its lower triangle for the factorisation
-        AJ_TRY(df_add_f64_lower(b.Fh, b.Fl, b.H, S, b.Ah, b.Al, b.da.Lh, b.da.Ll, st));
+        AJ_TRY(df_add_f64_sym(b.Fh, b.Fl, b.H, S, b.Ah, b.Al, b.da.Lh, b.da.Ll, st));
         // A and H share every factorisation launch (and, with the gradient, every inversion launch)
         const float* fh[2] = {b.da.Lh, b.dh.Lh};
         const float* fl[2] = {b.da.Ll, b.dh.Ll};

@@ -651,9 +651,13 @@ __global__ void df_zero_upper_kernel(float* __restrict__ h, float* __restrict__ 
         }
 }
 
-__global__ void df_logdet_kernel(const double* __restrict__ piv, int64_t S, double* __restrict__ out,
-                                 const int* info) {
+// log|A_z| = 2 sum_i log(pivot_i) for matrix z = blockIdx.x (out_z null: skipped)
+__global__ void df_logdet_kernel(const double* __restrict__ piv0, const double* __restrict__ piv1, int64_t S,
+                                 double* __restrict__ out0, double* __restrict__ out1, const int* info) {
     __shared__ double red[32];
+    const double* piv = blockIdx.x == 0 ? piv0 : piv1;
+    double* out = blockIdx.x == 0 ? out0 : out1;
+    if (!out) return;
     double acc = 0.0;
     for (int64_t i = threadIdx.x; i < S; i += blockDim.x) acc += log(piv[i]);
     acc = block_sum(acc, red);
@@ -1168,25 +1172,56 @@ int df_add_f64(const float* ah, const float* al, const double* b, int64_t n, flo
     return check_launch();
 }
 
-// o = a + b (S x S) and, in the same pass, its lower triangle with a zero upper triangle in lo_h/lo_l
-// (a factorisation's starting copy)
-__global__ void add_df_f64_lower_kernel(const float* __restrict__ ah, const float* __restrict__ al,
-                                        const double* __restrict__ b, int64_t S, float* __restrict__ oh,
-                                        float* __restrict__ ol, float* __restrict__ lo_h, float* __restrict__ lo_l) {
-    const int64_t n = S * S;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-        const df v = df_add({ah[t], al[t]}, df_from(b[t]));
-        oh[t] = v.hi;
-        ol[t] = v.lo;
-        const bool low = t % S <= t / S;
-        lo_h[t] = low ? v.hi : 0.f;
-        lo_l[t] = low ? v.lo : 0.f;
+// A = F + H from F's lower triangle, one 32 x 32 tile pair per block: lower tile (I, J), J <= I,
+// goes to A and to lo (the factorisation's starting copy); its transpose to A's tile (J, I) and
+// zeros to lo's.  A diagonal tile mirrors its own lower triangle.  So A is exactly symmetric.
+__global__ void __launch_bounds__(256)
+    add_df_f64_sym_kernel(const float* __restrict__ fh, const float* __restrict__ fl, const double* __restrict__ h,
+                          int64_t S, float* __restrict__ ah, float* __restrict__ al, float* __restrict__ lo_h,
+                          float* __restrict__ lo_l) {
+    __shared__ float th[32][33], tl[32][33];
+    int64_t ti, tj;
+    lower_tile_df(blockIdx.x, ti, tj);
+    const int64_t i0 = ti * 32, j0 = tj * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const bool diag = ti == tj;
+    for (int r = ty; r < 32; r += 8) {
+        const int64_t i = i0 + r, j = j0 + tx;
+        df v = {0.f, 0.f};
+        if (i < S && j < S && (!diag || tx <= r)) v = df_add({fh[i * S + j], fl[i * S + j]}, df_from(h[i * S + j]));
+        th[r][tx] = v.hi;
+        tl[r][tx] = v.lo;
     }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        const int64_t i = i0 + r, j = j0 + tx;
+        if (i < S && j < S) {
+            const bool low = !diag || tx <= r;
+            const float vh = low ? th[r][tx] : th[tx][r];
+            const float vl = low ? tl[r][tx] : tl[tx][r];
+            ah[i * S + j] = vh;
+            al[i * S + j] = vl;
+            lo_h[i * S + j] = low ? vh : 0.f;
+            lo_l[i * S + j] = low ? vl : 0.f;
+        }
+    }
+    if (!diag)
+        for (int r = ty; r < 32; r += 8) {
+            const int64_t i = j0 + r, j = i0 + tx;
+            if (i < S && j < S) {
+                ah[i * S + j] = th[tx][r];
+                al[i * S + j] = tl[tx][r];
+                lo_h[i * S + j] = 0.f;
+                lo_l[i * S + j] = 0.f;
+            }
+        }
 }
 
-int df_add_f64_lower(const float* ah, const float* al, const double* b, int64_t S, float* oh, float* ol, float* lo_h,
-                     float* lo_l, cudaStream_t st) {
-    add_df_f64_lower_kernel<<<blocks_for(S * S, 256, 8 * num_sms()), 256, 0, st>>>(ah, al, b, S, oh, ol, lo_h, lo_l);
+int df_add_f64_sym(const float* fh, const float* fl, const double* h, int64_t S, float* ah, float* al, float* lo_h,
+                   float* lo_l, cudaStream_t st) {
+    if (S <= 0) return AJ_OK;
+    const int64_t nt = (S + 31) / 32;
+    add_df_f64_sym_kernel<<<(unsigned)(nt * (nt + 1) / 2), 256, 0, st>>>(fh, fl, h, S, ah, al, lo_h, lo_l);
     return check_launch();
 }
 
@@ -1351,11 +1386,15 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
     }
     df_store_diag_kernel<<<dim3((unsigned)nbt, count), 256, 0, crit>>>(m, S);
     AJ_LAUNCHED();
-    for (int z = 0; z < count; ++z)
-        if (logdet && logdet[z]) {
-            df_logdet_kernel<<<1, 1024, 0, crit>>>(w[z]->piv, S, logdet[z], info);
-            AJ_LAUNCHED();
-        }
+    // the log-determinants need only the pivots: on the bulk lane, idle by now, beside the tails
+    // of the other lanes
+    if (logdet && (logdet[0] || (count > 1 && logdet[1]))) {
+        AJ_TRY(lane_signal(ln, kEvPanel, 0));
+        AJ_TRY(lane_wait(ln, 1, kEvPanel));
+        df_logdet_kernel<<<(unsigned)count, 1024, 0, bulk>>>(w[0]->piv, count > 1 ? w[1]->piv : nullptr, S, logdet[0],
+                                                             count > 1 ? logdet[1] : nullptr, info);
+        AJ_LAUNCHED();
+    }
     AJ_TRY(lanes_join(ln, st, nlanes));
     return AIh ? df_mirror_lower(AIh, AIl, S, st) : AJ_OK;
 }

@@ -256,10 +256,10 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(256)
     csc_spmm_t_df_kernel(const int* __restrict__ colptr, const int* __restrict__ rows, const float2* __restrict__ vdf,
                          const float* __restrict__ Xh, const float* __restrict__ Xl, int64_t ld_x, int64_t cols,
-                         float* __restrict__ Oh, float* __restrict__ Ol, int64_t ld_out) {
+                         float* __restrict__ Oh, float* __restrict__ Ol, int64_t ld_out, int lower) {
     const int64_t s = blockIdx.x;
     const int64_t c0 = (blockIdx.y * (int64_t)blockDim.x + threadIdx.x) * 4;
-    if (c0 >= cols) return;
+    if (c0 >= cols || (lower && c0 > s)) return;
     const int b = colptr[s], e = colptr[s + 1];
     df acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     for (int q = b; q < e; ++q) {
@@ -302,12 +302,13 @@ __global__ void __launch_bounds__(256)
     csc_spmm_t_df_vec_kernel(const int* __restrict__ colptr, const int* __restrict__ rows,
                              const float2* __restrict__ vdf, const float* __restrict__ Xh,
                              const float* __restrict__ Xl, int64_t ld_x, int64_t cols, float* __restrict__ Oh,
-                             float* __restrict__ Ol, int64_t ld_out) {
+                             float* __restrict__ Ol, int64_t ld_out, int lower) {
     __shared__ int srow[kGatherStage];
     __shared__ float2 sw[kGatherStage];
     const int64_t s = blockIdx.x;
+    if (lower && (int64_t)blockIdx.y * blockDim.x * 4 > s) return;  // the whole chunk is above the diagonal
     const int64_t c0 = (blockIdx.y * (int64_t)blockDim.x + threadIdx.x) * 4;
-    const bool live = c0 < cols;
+    const bool live = c0 < cols && (!lower || c0 <= s);
     const int b = colptr[s], e = colptr[s + 1];
     df acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     int group = 0;
@@ -636,7 +637,7 @@ template int csc_spmm_t<float, double>(const Csc&, int64_t, const float*, int64_
                                        cudaStream_t);
 
 int csc_spmm_t_df(const Csc& c, int64_t S, const float* Xh, const float* Xl, int64_t ld_x, int64_t cols, float* Oh,
-                  float* Ol, int64_t ld_out, cudaStream_t st) {
+                  float* Ol, int64_t ld_out, cudaStream_t st, bool lower) {
     if (S == 0 || cols == 0) return AJ_OK;
     // 512-column chunks: under 3% idle threads at both M = 9,504 and S = 1,500, and a chunk's
     // rows of X (M x 512 x 8 bytes) stay in L2 while every source pixel gathers from them
@@ -645,9 +646,11 @@ int csc_spmm_t_df(const Csc& c, int64_t S, const float* Xh, const float* Xl, int
                      (reinterpret_cast<uintptr_t>(Xh) % 16 == 0) && (reinterpret_cast<uintptr_t>(Xl) % 16 == 0) &&
                      (reinterpret_cast<uintptr_t>(Oh) % 16 == 0) && (reinterpret_cast<uintptr_t>(Ol) % 16 == 0);
     if (vec)
-        csc_spmm_t_df_vec_kernel<<<grid, 128, 0, st>>>(c.colptr, c.rows, c.vdf, Xh, Xl, ld_x, cols, Oh, Ol, ld_out);
+        csc_spmm_t_df_vec_kernel<<<grid, 128, 0, st>>>(c.colptr, c.rows, c.vdf, Xh, Xl, ld_x, cols, Oh, Ol, ld_out,
+                                                       lower ? 1 : 0);
     else
-        csc_spmm_t_df_kernel<<<grid, 128, 0, st>>>(c.colptr, c.rows, c.vdf, Xh, Xl, ld_x, cols, Oh, Ol, ld_out);
+        csc_spmm_t_df_kernel<<<grid, 128, 0, st>>>(c.colptr, c.rows, c.vdf, Xh, Xl, ld_x, cols, Oh, Ol, ld_out,
+                                                   lower ? 1 : 0);
     return check_launch();
 }
 
