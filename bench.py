@@ -44,7 +44,7 @@ METRIC = "logE+grad evals/s (mixed precision; K=1e6, M=9504, S=1500)"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--config", default="cfg3")
@@ -104,7 +104,7 @@ class Dist:
 class ClockSampler:
     """nvidia-smi clock/throttle samples during the timed region."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -120,38 +120,51 @@ class ClockSampler:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+                 "-lms", "20"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        # the timed region starts once the sampler is producing lines
+        t_end = time.time() + 3.0
+        while time.time() < t_end and self.path.stat().st_size == 0:
+            time.sleep(0.01)
 
-    def stop(self) -> dict:
+    def stop(self, t0: float | None = None, t1: float | None = None) -> dict:
+        """Summarise the samples taken between host times t0 and t1 (the timed region); if none
+        fell inside it, the nearest ones (the result says which)."""
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        time.sleep(0.25)
+        time.sleep(0.05)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.fh.close()
-        sm, smax, reasons = [], [], set()
-        names = ("active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        rows = []
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
         for line in self.path.read_text().splitlines():
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
-            except ValueError:
+                ts = time.mktime(time.strptime(parts[0].split(".")[0], "%Y/%m/%d %H:%M:%S"))
+                ts += float("0." + parts[0].split(".")[1]) if "." in parts[0] else 0.0
+                rows.append((ts, float(parts[2]), float(parts[3]),
+                             {n for n, v in zip(names, parts[6:10]) if v.lower() in ("active", "1", "0x1")}))
+            except (ValueError, IndexError):
                 continue
-            for name, val in zip(names[1:], parts[5:9]):
-                if val.lower() in ("active", "1", "0x1"):
-                    reasons.add(name)
-        if not sm:
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        inside = [r for r in rows if t0 is not None and t1 is not None and t0 <= r[0] <= t1]
+        where = "timed region"
+        if not inside:
+            mid = 0.5 * (t0 + t1) if t0 is not None and t1 is not None else rows[-1][0]
+            inside = sorted(rows, key=lambda r: abs(r[0] - mid))[:3]
+            where = "nearest to the timed region (none fell inside it)"
+        reasons = sorted(set().union(*(r[3] for r in inside)))
+        return {"sm_mhz": float(np.median([r[1] for r in inside])), "sm_max_mhz": max(r[2] for r in inside),
+                "reasons": reasons, "samples": len(inside), "sampled": where}
 
 
 def measured_peaks() -> dict:
@@ -390,8 +403,9 @@ def gpu_arm(args, dist: Dist) -> dict:
 
     clk = ClockSampler(dist.local)
     clk.start()
+    c0 = time.time()
     t_mixed = time_region(stepper(ev["mixed"]), args.steps, dist, "timed_mixed")
-    clocks = clk.stop()
+    clocks = clk.stop(c0, time.time())
     t_fp64 = time_region(stepper(ev["fp64"]), args.steps, dist, "timed_fp64")
     ev["mixed"].check()
 
