@@ -299,12 +299,35 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 // panel's rows), so the critical chain is one launch per step; the rest of
 // each trailing update runs on another lane.
 constexpr int PANEL_THREADS = 1024;
-constexpr int PANEL_RT = PANEL_THREADS / DNB;  // threads per row in the pre-update
-constexpr int PANEL_NC = DNB / PANEL_RT;       // columns per thread there
 constexpr int PANEL_SP = 8;  // sub-panel width of the panel factorisation
-static_assert(PANEL_THREADS == 32 * DNB && DNB % PANEL_SP == 0, "the pre-update gives each thread one column");
-// previous-panel rows as (hi, lo) pairs: the pivot block's 32 and this block's 64
-constexpr size_t PANEL_DYN_SMEM = sizeof(float2) * (32 + 64) * (32 + 1);
+static_assert(PANEL_THREADS >= 3 * 32 && DNB % PANEL_SP == 0, "three chain warps; whole sub-panels");
+constexpr int PRE_DIGITS = 6;  // 8-bit digits per double-float value in the tensor-core pre-update
+constexpr int PRE_LEVELS = 7;  // digit-product levels i + j kept
+constexpr int PRE_KS = DNB + 8;  // bf16 row stride of the digit planes: conflict-free fragment loads
+static_assert(PANEL_THREADS / 32 >= 3 * DNB / 16 * (DNB / 8), "one warp per 16 x 8 output tile");
+// previous-panel rows as (hi, lo) pairs (the pivot block's 32 and this block's 64), then their
+// digit planes
+constexpr size_t PANEL_DYN_SMEM = sizeof(float2) * (32 + 64) * (32 + 1) + sizeof(uint16_t) * PRE_DIGITS * 3 * DNB * PRE_KS;
+
+// x 2^k for k <= 252, exact unless the result leaves the normal range (two power-of-two factors
+// built from their exponent bits, each within the float range)
+__device__ __forceinline__ float scale2(float x, int k) {
+    if (k < -252) return x * 0.f;  // below the float range either way
+    const int k1 = k / 2;
+    return x * __int_as_float((k1 + 127) << 23) * __int_as_float((k - k1 + 127) << 23);
+}
+
+// d (16 x 8, float32) += a (16 x 16, bf16, row-major) b (16 x 8, bf16, column-major): one warp-wide
+// mma.sync; a thread holds a = {A[g][2t..], A[g+8][2t..], A[g][2t+8..], A[g+8][2t+8..]},
+// b = {B[2t..][g], B[2t+8..][g]} and d = {D[g][2t], D[g][2t+1], D[g+8][2t], D[g+8][2t+1]},
+// g = lane / 4, t = lane % 4, pairs packed low element first
+__device__ __forceinline__ void mma_bf16_16816(float* d, const uint32_t* a, const uint32_t* b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
 
 __global__ void __launch_bounds__(PANEL_THREADS)
     dfchol_panel_kernel(DfMats mats, int64_t S, int64_t k0, int pre, int* info) {
@@ -323,6 +346,8 @@ __global__ void __launch_bounds__(PANEL_THREADS)
     extern __shared__ float2 panel_dyn[];
     float2(*pdf)[DNB + 1] = reinterpret_cast<float2(*)[DNB + 1]>(panel_dyn);                    // P_k: 32 rows
     float2(*prf)[DNB + 1] = reinterpret_cast<float2(*)[DNB + 1]>(panel_dyn + DNB * (DNB + 1));  // P_r: 64 rows
+    uint16_t* xd = reinterpret_cast<uint16_t*>(panel_dyn + 3 * DNB * (DNB + 1));  // digits [i][row][k]
+    __shared__ int pexp[3 * DNB];  // row scales 2^e of the pre-update
     __shared__ int bad;
     const int tid = threadIdx.x;
     const bool rows = blockIdx.x > 0;
@@ -362,52 +387,81 @@ __global__ void __launch_bounds__(PANEL_THREADS)
     }
     __syncthreads();
     if (pre) {
-        // A_kk (lower) -= P_k P_k^T and rows -= P_r P_k^T; element (i, j) sums q over the 32 previous
-        // columns.  Thread (r, c) owns rows r (pivot block), r and r + 32 (panel rows) and column c:
-        // four (hi, lo) loads feed three multiply-adds per q.
-        const int r = tid / PANEL_RT, c = tid % PANEL_RT;
-        df acc[3][PANEL_NC];
+        // A_kk (lower) -= P_k P_k^T and rows -= P_r P_k^T, i.e. C = X Y^T with X = [P_k; P_r] (the
+        // previous panel's columns in this block's rows) and Y = P_k, on the tensor cores.  Each
+        // row of X is scaled by a power of two, |x| < 2^e, and cut into six signed 8-bit digits
+        // (x = 2^(e - 7) sum_i d_i 2^(-8 i), |d_i| <= 128, exact in bf16); the digit products of
+        // level L = i + j sum exactly in float32 (at most 6 x 32 x 2^14 < 2^24) and levels 0 .. 6
+        // fold back into double-float.  What is dropped is below 2^-43 of 2^(e_r + e_c), the
+        // rounding of a 32-term double-float dot product.
+        const int w = tid >> 5, lane = tid & 31;
+        for (int r = w; r < nrow; r += PANEL_THREADS / 32) {
+            const float2 v = r < DNB ? pdf[r][lane] : prf[r - DNB][lane];
+            float m = fabsf(v.x);
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
+            for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+            // e with m < 2^e from m's exponent bits (a subnormal or zero m takes the smallest)
+            const int be = (int)((__float_as_uint(m) >> 23) & 0xffu);
+            const int e = m > 0.f ? (be > 0 ? be - 126 : -126) : 0;
+            if (lane == 0) pexp[r] = e;
+            df t = {scale2(v.x, 7 - e), scale2(v.y, 7 - e)};
 #pragma unroll
-            for (int h = 0; h < PANEL_NC; ++h) acc[a][h] = {0.f, 0.f};
-#pragma unroll 8
-        for (int q = 0; q < DNB; ++q) {
-            float2 y[PANEL_NC];
-#pragma unroll
-            for (int h = 0; h < PANEL_NC; ++h) y[h] = pdf[c + PANEL_RT * h][q];
-            const float2 x0 = pdf[r][q];
-#pragma unroll
-            for (int h = 0; h < PANEL_NC; ++h) df_fma_lazy(acc[0][h], {x0.x, x0.y}, {y[h].x, y[h].y});
-            if (rows) {
-                const float2 x1 = prf[r][q], x2 = prf[r + 32][q];
-#pragma unroll
-                for (int h = 0; h < PANEL_NC; ++h) {
-                    df_fma_lazy(acc[1][h], {x1.x, x1.y}, {y[h].x, y[h].y});
-                    df_fma_lazy(acc[2][h], {x2.x, x2.y}, {y[h].x, y[h].y});
-                }
+            for (int i = 0; i < PRE_DIGITS; ++i) {
+                const float d = rintf(t.hi);  // an integer of at most 8 bits: its bf16 is the top half
+                xd[(i * 3 * DNB + r) * PRE_KS + lane] = (uint16_t)(__float_as_uint(d) >> 16);
+                float hs, he;
+                two_sum(t.hi - d, t.lo, hs, he);
+                t = {hs * 256.f, he * 256.f};
             }
-            if ((q & 7) == 7)
-#pragma unroll
-                for (int a = 0; a < 3; ++a)
-#pragma unroll
-                    for (int h = 0; h < PANEL_NC; ++h) df_renorm(acc[a][h]);
         }
+        __syncthreads();
+        // 16 x 8 output tiles, one a warp: rows R0 .., columns C0 ..
+        if (w < (nrow / 16) * (DNB / 8)) {
+            const int R0 = (w / (DNB / 8)) * 16, C0 = (w % (DNB / 8)) * 8;
+            const int g = lane >> 2, tq = lane & 3;
+            float acc[PRE_LEVELS][4];
 #pragma unroll
-        for (int h = 0; h < PANEL_NC; ++h) {
-            const int j = c + PANEL_RT * h;
-            if (j <= r && r < nb && j < nb) {
-                const df v = df_add({ph[r][j], pl[r][j]}, df_neg(acc[0][h]));
-                ph[r][j] = v.hi;
-                pl[r][j] = v.lo;
-            }
-            if (rows) {
-                const df v1 = df_add({ph[DNB + r][j], pl[DNB + r][j]}, df_neg(acc[1][h]));
-                ph[DNB + r][j] = v1.hi;
-                pl[DNB + r][j] = v1.lo;
-                const df v2 = df_add({ph[DNB + r + 32][j], pl[DNB + r + 32][j]}, df_neg(acc[2][h]));
-                ph[DNB + r + 32][j] = v2.hi;
-                pl[DNB + r + 32][j] = v2.lo;
+            for (int L = 0; L < PRE_LEVELS; ++L)
+#pragma unroll
+                for (int o = 0; o < 4; ++o) acc[L][o] = 0.f;
+#pragma unroll
+            for (int i = 0; i < PRE_DIGITS; ++i)
+#pragma unroll
+                for (int j = 0; j < PRE_DIGITS; ++j) {
+                    if (i + j >= PRE_LEVELS) continue;
+                    const uint16_t* A = xd + i * 3 * DNB * PRE_KS;
+                    const uint16_t* Bm = xd + j * 3 * DNB * PRE_KS;
+#pragma unroll
+                    for (int ks = 0; ks < DNB; ks += 16) {
+                        uint32_t a[4], b[2];
+                        a[0] = *reinterpret_cast<const uint32_t*>(A + (R0 + g) * PRE_KS + ks + 2 * tq);
+                        a[1] = *reinterpret_cast<const uint32_t*>(A + (R0 + g + 8) * PRE_KS + ks + 2 * tq);
+                        a[2] = *reinterpret_cast<const uint32_t*>(A + (R0 + g) * PRE_KS + ks + 2 * tq + 8);
+                        a[3] = *reinterpret_cast<const uint32_t*>(A + (R0 + g + 8) * PRE_KS + ks + 2 * tq + 8);
+                        b[0] = *reinterpret_cast<const uint32_t*>(Bm + (C0 + g) * PRE_KS + ks + 2 * tq);
+                        b[1] = *reinterpret_cast<const uint32_t*>(Bm + (C0 + g) * PRE_KS + ks + 2 * tq + 8);
+                        mma_bf16_16816(acc[i + j], a, b);
+                    }
+                }
+            // accumulator o holds (R0 + g (+ 8 for o >= 2), C0 + 2 tq + (o & 1))
+#pragma unroll
+            for (int o = 0; o < 4; ++o) {
+                const int r = R0 + g + (o >= 2 ? 8 : 0), c = C0 + 2 * tq + (o & 1);
+                // levels 3 .. 6 are below 2^-24 of level 0, so their float sum rounds at the
+                // 2^-48 level; levels 0 .. 2 and that tail add as double-float
+                float tail = 0.f;
+#pragma unroll
+                for (int L = PRE_LEVELS - 1; L >= 3; --L) tail += acc[L][o] * __int_as_float((127 - 8 * L) << 23);
+                df sum = {tail, 0.f};
+#pragma unroll
+                for (int L = 2; L >= 0; --L) sum = df_add(sum, {acc[L][o] * __int_as_float((127 - 8 * L) << 23), 0.f});
+                const int sc = pexp[r] + pexp[c] - 14;
+                sum = {scale2(sum.hi, sc), scale2(sum.lo, sc)};
+                if (r >= DNB || (c <= r && r < nb && c < nb)) {
+                    const df v = df_add({ph[r][c], pl[r][c]}, df_neg(sum));
+                    ph[r][c] = v.hi;
+                    pl[r][c] = v.lo;
+                }
             }
         }
     }
