@@ -304,7 +304,6 @@ static_assert(PANEL_THREADS >= 3 * 32 && DNB % PANEL_SP == 0, "three chain warps
 constexpr int PRE_DIGITS = 6;  // 8-bit digits per double-float value in the tensor-core pre-update
 constexpr int PRE_LEVELS = 7;  // digit-product levels i + j kept
 constexpr int PRE_KS = DNB + 8;  // bf16 row stride of the digit planes: conflict-free fragment loads
-static_assert(PANEL_THREADS / 32 >= 3 * DNB / 16 * (DNB / 8), "one warp per 16 x 8 output tile");
 // previous-panel rows as (hi, lo) pairs (the pivot block's 32 and this block's 64), then their
 // digit planes
 constexpr size_t PANEL_DYN_SMEM = sizeof(float2) * (32 + 64) * (32 + 1) + sizeof(uint16_t) * PRE_DIGITS * 3 * DNB * PRE_KS;
@@ -415,9 +414,9 @@ __global__ void __launch_bounds__(PANEL_THREADS)
             }
         }
         __syncthreads();
-        // 16 x 8 output tiles, one a warp: rows R0 .., columns C0 ..
-        if (w < (nrow / 16) * (DNB / 8)) {
-            const int R0 = (w / (DNB / 8)) * 16, C0 = (w % (DNB / 8)) * 8;
+        // 16 x 8 output tiles spread over the warps: rows R0 .., columns C0 ..
+        for (int tile = w; tile < (nrow / 16) * (DNB / 8); tile += PANEL_THREADS / 32) {
+            const int R0 = (tile / (DNB / 8)) * 16, C0 = (tile % (DNB / 8)) * 8;
             const int g = lane >> 2, tq = lane & 3;
             float acc[PRE_LEVELS][4];
 #pragma unroll
