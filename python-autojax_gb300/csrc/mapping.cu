@@ -358,10 +358,13 @@ __global__ void __launch_bounds__(256)
 }
 
 // The same gather with the output transposed (out[c][s], e.g. Omega = (T^T W)^T): a block takes
-// 8 source pixels over one 512-column chunk, one pixel after another with the entry order, the
+// 4 source pixels over one 512-column chunk, one pixel after another with the entry order, the
 // grouping and the renormalisation of csc_spmm_t_df_vec_kernel (so each sum is bit-identical),
-// keeps the results in shared memory and stores 8 consecutive pixels (32 bytes) per output row.
-constexpr int kTrPix = 8;
+// keeps the results in shared memory and stores 4 consecutive pixels (16 bytes) per output row.
+// With the grid pixel-fastest, (threads in flight x 4 columns x 4 pixels) / S columns of X are
+// live, about 63 MB at M = 9,504, S = 1,500, inside L2; 8 pixels a block (32-byte stores) kept
+// twice that and read X 1.95 times from DRAM, 60 us slower per evaluation.
+constexpr int kTrPix = 4;
 constexpr int kTrCols = 512;
 
 __global__ void __launch_bounds__(128)
@@ -440,9 +443,7 @@ __global__ void __launch_bounds__(128)
         float* ol = Ol + c * ld_out + s0;
         if (vec) {
             reinterpret_cast<float4*>(oh)[0] = make_float4(th[0][r], th[1][r], th[2][r], th[3][r]);
-            reinterpret_cast<float4*>(oh)[1] = make_float4(th[4][r], th[5][r], th[6][r], th[7][r]);
             reinterpret_cast<float4*>(ol)[0] = make_float4(tl[0][r], tl[1][r], tl[2][r], tl[3][r]);
-            reinterpret_cast<float4*>(ol)[1] = make_float4(tl[4][r], tl[5][r], tl[6][r], tl[7][r]);
         } else {
             for (int sp = 0; sp < np; ++sp) {
                 oh[sp] = th[sp][r];
