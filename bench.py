@@ -246,9 +246,9 @@ def time_region(fn, steps: int, dist: Dist, name: str = "region") -> float:
 
 # DRAM bytes (read + write) of one aj_spd_inverse_mixed call at S = 1,500, summed
 # over its launches, from the warm-cache ncu capture in
-# profiles/spd_inverse_mixed_s1500_traffic.md (15.9 MB read, 58.8 MB written):
+# profiles/spd_inverse_mixed_s1500_traffic.md (16.0 MB read, 56.9 MB written):
 # the group's working set, 7 double-float S x S planes (63 MB), stays in L2.
-ROOFLINE_TRAFFIC_BYTES = 74.7e6
+ROOFLINE_TRAFFIC_BYTES = 72.9e6
 
 
 def roofline(A, dist: Dist):
