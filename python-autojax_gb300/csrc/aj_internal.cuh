@@ -37,7 +37,7 @@ int spd_inverse_from_factor(int64_t S, SpdWorkspace& w, double* Ainv, cudaStream
 
 // ---- lanes.cu (side streams that fork from and join back into the caller's stream)
 
-// 0: critical chain (highest priority), 1: bulk updates, 2: triangular inverse
+// 0: critical chain (highest priority; the others share the next), 1: bulk updates, 2: triangular inverse
 // of the first matrix, 3: triangular inverse of the second, 4: A^-1 of the first
 constexpr int kLaneCount = 5;
 enum LaneEvent {
