@@ -234,3 +234,59 @@ def test_tile_policy_does_not_change_results():
         tune.set_tile_policy(*saved)
     for inv, ld in outs[1:]:
         assert torch.equal(inv, outs[0][0]) and torch.equal(ld, outs[0][1])
+
+
+def _spd_inverse_mixed(A):
+    import torch
+
+    from autojax_gb300 import _lib
+
+    lib = _lib.load()
+    S = A.shape[0]
+    At = torch.from_numpy(np.ascontiguousarray(A)).cuda()
+    inv = torch.empty_like(At)
+    logdet = torch.zeros(1, dtype=torch.float64, device="cuda")
+    info = torch.zeros(2, dtype=torch.int32, device="cuda")
+    ws = torch.empty(lib.aj_spd_inverse_mixed_workspace_size(S), dtype=torch.uint8, device="cuda")
+    _lib.check(lib.aj_spd_inverse_mixed(At.data_ptr(), S, inv.data_ptr(), logdet.data_ptr(), ws.data_ptr(),
+                                        ws.numel(), info.data_ptr(), torch.cuda.current_stream().cuda_stream),
+               "aj_spd_inverse_mixed")
+    torch.cuda.synchronize()
+    assert int(info[0]) == 0
+    return inv.cpu().numpy(), float(logdet[0])
+
+
+@pytest.mark.parametrize("S", [96, 257, 500])
+def test_mixed_spd_inverse_graded(S):
+    """A = D B D with D spanning 1e-3 .. 1e3 (a graded matrix, cond(A) ~ 1e12 cond(B)).
+
+    The panel's pre-update cuts each row of L into 8-bit digits relative to that row's largest
+    entry; L = D chol(B) is graded by rows only, so the factorisation keeps the accuracy of B:
+    each entry of A^-1 = D^-1 B^-1 D^-1 to ~S 2^-47 cond(B) of its own scale max|B^-1| / (d_i d_j),
+    and log|A| to ~S 2^-47 cond(B).
+    """
+    cond = 1e6
+    B = _spd_with_condition(S, cond, 101 + S)
+    d = np.logspace(-3.0, 3.0, S)[np.random.default_rng(5).permutation(S)]
+    A = (d[:, None] * B) * d[None, :]
+    got, ld = _spd_inverse_mixed(A)
+    ref = (np.linalg.inv(B) / d[:, None]) / d[None, :]
+    scale = np.abs(np.linalg.inv(B)).max() / np.outer(d, d)
+    tol = max(S, 32) * 2.0**-47 * cond
+    assert np.max(np.abs(got - ref) / scale) <= tol
+    ld_ref = np.linalg.slogdet(B)[1] + 2.0 * np.log(d).sum()
+    assert abs(ld - ld_ref) <= tol * max(1.0, abs(ld_ref))
+
+
+def test_mixed_spd_inverse_ill_conditioned():
+    """cond(A) = 1e10 at S = 500 (16 panels through the tensor-core pre-update): the inverse to
+    ~S 2^-47 cond(A) of its largest entry and log|A| to ~S 2^-47 cond(A), as for a double-float
+    factorisation."""
+    S, cond = 500, 1e10
+    A = _spd_with_condition(S, cond, 77)
+    got, ld = _spd_inverse_mixed(A)
+    ref = np.linalg.inv(A)
+    tol = S * 2.0**-47 * cond
+    assert np.abs(got - ref).max() <= tol * np.abs(ref).max()
+    # |d log|A|| = |tr(A^-1 dA)| <= S cond(A) |dA| / |A|
+    assert abs(ld - np.linalg.slogdet(A)[1]) <= S * 2.0**-47 * cond
