@@ -38,8 +38,9 @@ int spd_inverse_from_factor(int64_t S, SpdWorkspace& w, double* Ainv, cudaStream
 // ---- lanes.cu (side streams that fork from and join back into the caller's stream)
 
 // 0: critical chain (highest priority; the others share the next), 1: bulk updates, 2: triangular inverse
-// of the first matrix, 3: triangular inverse of the second, 4: A^-1 of the first
-constexpr int kLaneCount = 5;
+// of the first matrix, 3: triangular inverse of the second, 4: A^-1 of the first; 5: a second
+// factorisation running beside the first (never forked or joined by it)
+constexpr int kLaneCount = 6;
 enum LaneEvent {
     kEvFork = 0,
     kEvPanel,
@@ -48,6 +49,7 @@ enum LaneEvent {
     kEvRow,      // a block row of the first matrix's L^-1 is final
     kEvPre,      // the evaluation's independent pre-work forks here ...
     kEvPreDone,  // ... and is joined here
+    kEvHDone,    // H's factorisation, beside A's, is done
     kEvJoin0,
     kLaneEvents = kEvJoin0 + kLaneCount
 };

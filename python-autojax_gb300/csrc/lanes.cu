@@ -18,6 +18,7 @@
 // own, so their chains stay concurrent and never share an event.
 
 #include <map>
+#include <set>
 #include <mutex>
 
 #include "aj_internal.cuh"
@@ -28,12 +29,15 @@ namespace {
 
 std::mutex g_lanes_mu;
 std::map<std::pair<int, cudaStream_t>, Lanes*> g_lanes;
+std::set<std::pair<int, cudaStream_t>> g_side;  // every lane stream created here
 
-int create_lanes(Lanes& l) {
+// Lanes forked from another set's lane (a factorisation running beside the main one) are all
+// at the side priority, so their chain stays below the main chain's panels.
+int create_lanes(Lanes& l, bool background) {
     int least = 0, greatest = 0;
     if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return AJ_ERR_CUDA;
     const int mid = greatest < least ? greatest + 1 : least;
-    const int prio[kLaneCount] = {greatest, mid, mid, mid, mid};
+    const int prio[kLaneCount] = {background ? mid : greatest, mid, mid, mid, mid, mid};
     for (int i = 0; i < kLaneCount; ++i)
         if (cudaStreamCreateWithPriority(&l.s[i], cudaStreamNonBlocking, prio[i]) != cudaSuccess) return AJ_ERR_CUDA;
     for (int i = 0; i < kLaneEvents; ++i)
@@ -50,12 +54,13 @@ int lanes_for(cudaStream_t caller, Lanes** out) {
     auto it = g_lanes.find({dev, caller});
     if (it == g_lanes.end()) {
         Lanes* l = new Lanes{};
-        const int rc = create_lanes(*l);
+        const int rc = create_lanes(*l, g_side.count({dev, caller}) != 0);
         if (rc != AJ_OK) {
             g_last_cuda_error = static_cast<int>(cudaGetLastError());
             delete l;  // streams or events created before the failure stay with the context
             return rc;
         }
+        for (int i = 0; i < kLaneCount; ++i) g_side.insert({dev, l->s[i]});
         it = g_lanes.emplace(std::make_pair(dev, caller), l).first;
     }
     *out = it->second;

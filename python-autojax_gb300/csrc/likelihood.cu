@@ -501,6 +501,22 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
             cudaStreamWaitEvent(st, ln.ev[kEvPreDone], 0);
             return rc;
         }
+        if (mixed) {
+            // H's factorisation (and, with the gradient, its L^-1 for tr(H^-1)) beside A's, from
+            // lane 5: its own lanes fork from there, so its panels run below A's
+            cudaStream_t hlane = ln.s[5];
+            if (cudaStreamWaitEvent(hlane, ln.ev[kEvPreDone], 0) != cudaSuccess) return AJ_ERR_CUDA;
+            const float* hh[1] = {b.dh.Lh};
+            const float* hl[1] = {b.dh.Ll};
+            DfSpd* hw[1] = {&b.dh};
+            double* hld[1] = {b.logdets + 1};
+            rc = dfspd_factor_invert_n(hh, hl, 1, with_grad ? 1 : 0, S, hw, hld, info, hlane, nullptr, nullptr, true);
+            if (cudaEventRecord(ln.ev[kEvHDone], hlane) != cudaSuccess) return AJ_ERR_CUDA;
+            if (rc != AJ_OK) {
+                cudaStreamWaitEvent(st, ln.ev[kEvHDone], 0);
+                return rc;
+            }
+        }
     }
     auto join_pre = [&]() {
         return cudaStreamWaitEvent(st, ln.ev[kEvPreDone], 0) == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
@@ -544,15 +560,17 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         AJ_TRY(csc_spmm_t_df(b.cs, S, b.Omh, b.Oml, S, S, b.Fh, b.Fl, S, st, true));
         AJ_TRY(join_pre());
         AJ_TRY(df_add_f64_sym(b.Fh, b.Fl, b.H, S, b.Ah, b.Al, b.da.Lh, b.da.Ll, st));
-        // A and H share every factorisation launch (and, with the gradient, every inversion launch)
-        const float* fh[2] = {b.da.Lh, b.dh.Lh};
-        const float* fl[2] = {b.da.Ll, b.dh.Ll};
-        DfSpd* fw[2] = {&b.da, &b.dh};
-        double* ld[2] = {b.logdets + 0, b.logdets + 1};
-        AJ_TRY(dfspd_factor_invert_n(fh, fl, 2, with_grad ? 2 : 1, S, fw, ld, info, st, with_grad ? b.AIh : nullptr,
+        // A's factorisation, L^-1 and (with the gradient) A^-1 on this stream's lanes; H's runs
+        // beside it from the side lane
+        const float* fh[1] = {b.da.Lh};
+        const float* fl[1] = {b.da.Ll};
+        DfSpd* fw[1] = {&b.da};
+        double* ld[1] = {b.logdets + 0};
+        AJ_TRY(dfspd_factor_invert_n(fh, fl, 1, 1, S, fw, ld, info, st, with_grad ? b.AIh : nullptr,
                                      with_grad ? b.AIl : nullptr, true));
         AJ_TRY(dfspd_solve_refined(S, b.da, b.Ah, b.Al, b.D, b.s, b.res, st, with_grad ? b.AIh : nullptr,
                                    with_grad ? b.AIl : nullptr));
+        if (cudaStreamWaitEvent(st, ln.ev[kEvHDone], 0) != cudaSuccess) return AJ_ERR_CUDA;
     }
 
     // logE from the chi^2 and log-noise sums (side lane), s.D and the log-determinants
