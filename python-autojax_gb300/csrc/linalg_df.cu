@@ -22,8 +22,8 @@ namespace aj {
 constexpr int DNB = 32;
 
 // Up to two independent matrices factored or inverted by the same launches
-// (blockIdx.y picks one): the evaluation's A and H share every step, which
-// halves the serial chain of small launches and doubles their parallelism.
+// (blockIdx.y picks one).  The evaluation factors A and H separately, H on
+// lanes of its own beside A's (likelihood.cu), so each launch carries one.
 struct DfMats {
     float* Lh[2];
     float* Ll[2];
