@@ -18,7 +18,6 @@
 // own, so their chains stay concurrent and never share an event.
 
 #include <map>
-#include <set>
 #include <mutex>
 
 #include "aj_internal.cuh"
@@ -29,15 +28,15 @@ namespace {
 
 std::mutex g_lanes_mu;
 std::map<std::pair<int, cudaStream_t>, Lanes*> g_lanes;
-std::set<std::pair<int, cudaStream_t>> g_side;  // every lane stream created here
 
-// Lanes forked from another set's lane (a factorisation running beside the main one) are all
-// at the side priority, so their chain stays below the main chain's panels.
-int create_lanes(Lanes& l, bool background) {
+// Every set the same, including one forked from another set's lane (H's factorisation beside
+// A's): its panel chain at the top priority too measured 9 us per evaluation faster than at the
+// side priority, and 87 us faster than at the lowest.
+int create_lanes(Lanes& l) {
     int least = 0, greatest = 0;
     if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return AJ_ERR_CUDA;
     const int mid = greatest < least ? greatest + 1 : least;
-    const int prio[kLaneCount] = {background ? mid : greatest, mid, mid, mid, mid, mid};
+    const int prio[kLaneCount] = {greatest, mid, mid, mid, mid, mid};
     for (int i = 0; i < kLaneCount; ++i)
         if (cudaStreamCreateWithPriority(&l.s[i], cudaStreamNonBlocking, prio[i]) != cudaSuccess) return AJ_ERR_CUDA;
     for (int i = 0; i < kLaneEvents; ++i)
@@ -54,13 +53,12 @@ int lanes_for(cudaStream_t caller, Lanes** out) {
     auto it = g_lanes.find({dev, caller});
     if (it == g_lanes.end()) {
         Lanes* l = new Lanes{};
-        const int rc = create_lanes(*l, g_side.count({dev, caller}) != 0);
+        const int rc = create_lanes(*l);
         if (rc != AJ_OK) {
             g_last_cuda_error = static_cast<int>(cudaGetLastError());
             delete l;  // streams or events created before the failure stay with the context
             return rc;
         }
-        for (int i = 0; i < kLaneCount; ++i) g_side.insert({dev, l->s[i]});
         it = g_lanes.emplace(std::make_pair(dev, caller), l).first;
     }
     *out = it->second;

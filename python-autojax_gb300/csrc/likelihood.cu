@@ -503,7 +503,7 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         }
         if (mixed) {
             // H's factorisation (and, with the gradient, its L^-1 for tr(H^-1)) beside A's, from
-            // lane 5: its own lanes fork from there, so its panels run below A's
+            // lane 5 (which A's factorisation never forks or joins), on lanes of its own
             cudaStream_t hlane = ln.s[5];
             if (cudaStreamWaitEvent(hlane, ln.ev[kEvPreDone], 0) != cudaSuccess) return AJ_ERR_CUDA;
             const float* hh[1] = {b.dh.Lh};
