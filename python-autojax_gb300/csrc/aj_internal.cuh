@@ -50,6 +50,7 @@ enum LaneEvent {
     kEvPre,      // the evaluation's independent pre-work forks here ...
     kEvPreDone,  // ... and is joined here
     kEvHDone,    // H's factorisation, beside A's, is done
+    kEvHReady,   // H is split and its inverse buffer zeroed
     kEvJoin0,
     kLaneEvents = kEvJoin0 + kLaneCount
 };

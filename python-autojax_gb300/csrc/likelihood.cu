@@ -487,6 +487,8 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
                     rc = AJ_ERR_CUDA;
             }
         }
+        // H's factorisation (below) can start here, before the chi^2 and log-noise sums
+        if (cudaEventRecord(ln.ev[kEvHReady], pre) != cudaSuccess) return AJ_ERR_CUDA;
         if (rc == AJ_OK) {
             if (K > 0) {
                 k_terms_kernel<<<(unsigned)b.nk_blocks, KT_THREADS, 0, pre>>>(p->data, p->noise_map, 2 * K, b.kpart);
@@ -505,7 +507,7 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
             // H's factorisation (and, with the gradient, its L^-1 for tr(H^-1)) beside A's, from
             // lane 5 (which A's factorisation never forks or joins), on lanes of its own
             cudaStream_t hlane = ln.s[5];
-            if (cudaStreamWaitEvent(hlane, ln.ev[kEvPreDone], 0) != cudaSuccess) return AJ_ERR_CUDA;
+            if (cudaStreamWaitEvent(hlane, ln.ev[kEvHReady], 0) != cudaSuccess) return AJ_ERR_CUDA;
             const float* hh[1] = {b.dh.Lh};
             const float* hl[1] = {b.dh.Ll};
             DfSpd* hw[1] = {&b.dh};
