@@ -84,7 +84,6 @@ DfSpd dfspd_carve(Carver& cv, int64_t S, bool with_inverse);
 int df_split(const double* x, int64_t n, float* hi, float* lo, cudaStream_t st);
 int df_mirror_lower(float* hi, float* lo, int64_t S, cudaStream_t st);
 int df_join(const float* hi, const float* lo, int64_t n, double* x, cudaStream_t st);
-int df_add_f64(const float* ah, const float* al, const double* b, int64_t n, float* oh, float* ol, cudaStream_t st);
 // A = F + H (S x S) from F's lower triangle (F planes, H float64): A symmetric in full, and its
 // lower triangle, upper zero, in lo_h/lo_l
 int df_add_f64_sym(const float* fh, const float* fl, const double* h, int64_t S, float* ah, float* al, float* lo_h,
@@ -92,8 +91,8 @@ int df_add_f64_sym(const float* fh, const float* fl, const double* h, int64_t S,
 int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const float* Ah, const float* Al, int64_t lda,
             const float* Bh, const float* Bl, int64_t ldb, bool accumulate, float* Ch, float* Cl, int64_t ldc,
             bool lower_only, bool tri_k, cudaStream_t st);
-int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* logdet, int* info, cudaStream_t st);
-// The same for count = 1 or 2 independent matrices sharing every launch; the
+// Double-float Cholesky L (in w[z]) with log|A| of count = 1 or 2 independent
+// S x S matrices (planes) sharing every launch; the
 // first n_inverse of them also get their inverse factor L^-1 (in w->Ih/Il),
 // computed alongside the factorisation as its panels complete.  With AIh/AIl
 // set (planes, S x S), the first matrix's inverse A^-1 = L^-T L^-1 is built

@@ -107,17 +107,6 @@ __global__ void join_kernel(const float* __restrict__ hi, const float* __restric
         x[t] = (double)hi[t] + (double)lo[t];
 }
 
-// (hi, lo) = df(a) + df(b) for float64 a (plane pair given) and double b
-__global__ void add_df_f64_kernel(const float* __restrict__ ah, const float* __restrict__ al,
-                                  const double* __restrict__ b, int64_t n, float* __restrict__ oh,
-                                  float* __restrict__ ol) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-        const df v = df_add({ah[t], al[t]}, df_from(b[t]));
-        oh[t] = v.hi;
-        ol[t] = v.lo;
-    }
-}
-
 // ------------------------------------------------------------------- GEMM
 
 // C (m x n) = (neg ? -1 : 1) op(A) op(B) (+ C when accumulate), double-float planes.
@@ -1220,11 +1209,6 @@ int df_join(const float* hi, const float* lo, int64_t n, double* x, cudaStream_t
     return check_launch();
 }
 
-int df_add_f64(const float* ah, const float* al, const double* b, int64_t n, float* oh, float* ol, cudaStream_t st) {
-    add_df_f64_kernel<<<blocks_for(n, 256, 8 * num_sms()), 256, 0, st>>>(ah, al, b, n, oh, ol);
-    return check_launch();
-}
-
 // A = F + H from F's lower triangle, one 32 x 32 tile pair per block: lower tile (I, J), J <= I,
 // goes to A and to lo (the factorisation's starting copy); its transpose to A's tile (J, I) and
 // zeros to lo's.  A diagonal tile mirrors its own lower triangle.  So A is exactly symmetric.
@@ -1450,12 +1434,6 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
     }
     AJ_TRY(lanes_join(ln, st, nlanes));
     return AIh ? df_mirror_lower(AIh, AIl, S, st) : AJ_OK;
-}
-
-int dfspd_factor(const float* Ah, const float* Al, int64_t S, DfSpd& w, double* logdet, int* info, cudaStream_t st) {
-    DfSpd* ws[1] = {&w};
-    double* ld[1] = {logdet};
-    return dfspd_factor_invert_n(&Ah, &Al, 1, 0, S, ws, ld, info, st, nullptr, nullptr);
 }
 
 // x = A^-1 b = Li^T (Li b) with the inverse factor, b and x may alias.  The
