@@ -100,10 +100,11 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int count, int n_inverse, int64_t S,
                           DfSpd* const* w, double* const* logdet, int* info, cudaStream_t st, float* AIh = nullptr,
                           float* AIl = nullptr, bool prepared = false);
-// x = A^-1 b through the inverse factor (two triangular products)
-int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st);
-int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x, double* r,
-                        cudaStream_t st, const float* AIh = nullptr, const float* AIl = nullptr);
+// x = A^-1 b refined once against A (planes), the correction through A^-1's planes when given;
+// b_split: b's planes are already in w.vec; xh/xl, when set, receive x's planes
+int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x,
+                        cudaStream_t st, const float* AIh = nullptr, const float* AIl = nullptr, bool b_split = false,
+                        float* xh = nullptr, float* xl = nullptr);
 int df_frob_lower(const float* h, const float* l, int64_t S, double* partial, int64_t nparts, cudaStream_t st);
 
 // ---- mapping.cu

@@ -314,7 +314,7 @@ struct EvidenceBufs {
     Csc ca{}, cs{};
     SpdWorkspace wa{}, wh{};          // float64 path
     DfSpd da{}, dh{};                 // mixed path
-    double *TW, *Om, *F, *H, *A, *Ainv, *D, *s, *res, *kpart, *fpart, *logdets;
+    double *TW, *Om, *F, *H, *A, *Ainv, *D, *s, *kpart, *fpart, *logdets;
     float *Wh, *Wl;                   // w_tilde planes when split per call
     float *TWh, *TWl, *Omh, *Oml, *Fh, *Fl, *Ah, *Al, *AIh, *AIl, *sh, *sl;
     int64_t nk_blocks, nfrob;
@@ -349,7 +349,6 @@ size_t evidence_carve(const aj_problem* p, bool mixed, bool with_grad, void* bas
     b.H = cv.take<double>(S * S);
     b.D = cv.take<double>(S);
     b.s = cv.take<double>(S);
-    b.res = cv.take<double>(S);
     b.kpart = cv.take<double>(2 * b.nk_blocks);
     b.fpart = cv.take<double>(b.nfrob);
     b.logdets = cv.take<double>(8);
@@ -496,6 +495,11 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
             } else if (cudaMemsetAsync(b.kpart, 0, sizeof(double) * 2 * b.nk_blocks, pre) != cudaSuccess) {
                 rc = AJ_ERR_CUDA;
             }
+            // D's planes for the solve, in A's solve scratch (which its factorisation leaves alone)
+            if (rc == AJ_OK && mixed) {
+                float* dp = reinterpret_cast<float*>(b.da.vec);
+                rc = df_split(b.D, S, dp, dp + S, pre);
+            }
         }
         // joined even after a failed enqueue, so st never runs ahead of the side lane
         if (cudaEventRecord(ln.ev[kEvPreDone], pre) != cudaSuccess) return AJ_ERR_CUDA;
@@ -570,8 +574,10 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         double* ld[1] = {b.logdets + 0};
         AJ_TRY(dfspd_factor_invert_n(fh, fl, 1, 1, S, fw, ld, info, st, with_grad ? b.AIh : nullptr,
                                      with_grad ? b.AIl : nullptr, true));
-        AJ_TRY(dfspd_solve_refined(S, b.da, b.Ah, b.Al, b.D, b.s, b.res, st, with_grad ? b.AIh : nullptr,
-                                   with_grad ? b.AIl : nullptr));
+        // (with the gradient, s's planes for the adjoint come out of the solve's last product)
+        AJ_TRY(dfspd_solve_refined(S, b.da, b.Ah, b.Al, b.D, b.s, st, with_grad ? b.AIh : nullptr,
+                                   with_grad ? b.AIl : nullptr, true, with_grad ? b.sh : nullptr,
+                                   with_grad ? b.sl : nullptr));
         if (cudaStreamWaitEvent(st, ln.ev[kEvHDone], 0) != cudaSuccess) return AJ_ERR_CUDA;
     }
 
@@ -591,8 +597,6 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         AJ_TRY(spd_invert_factor(S, b.wh, info, st));
         frob_lower_kernel<<<(unsigned)b.nfrob, 256, 0, st>>>(b.wh.Linv, S, b.fpart);
         AJ_LAUNCHED();
-    } else {
-        AJ_TRY(df_split(b.s, S, b.sh, b.sl, st));
     }
     // dlogE/dlambda (and, mixed, tr(H^-1)'s partial sums) on the side lane while st computes
     // the weight gradient; both read only finished data

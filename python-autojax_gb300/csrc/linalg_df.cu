@@ -1035,8 +1035,10 @@ __global__ void df_mirror_lower_kernel(float* __restrict__ h, float* __restrict_
         }
 }
 
-// Output of a matrix-vector product: float64 and, when yh is set, double-float planes.
-__device__ __forceinline__ void store_y(double v, int64_t i, double* y, float* yh, float* yl) {
+// Output of a matrix-vector product: float64 and, when yh is set, double-float planes;
+// with add the product is added to y (read first) and the sum is stored.
+__device__ __forceinline__ void store_y(double v, int64_t i, double* y, float* yh, float* yl, bool add = false) {
+    if (add) v = y[i] + v;
     if (y) y[i] = v;
     if (yh) {
         const df d = df_from(v);
@@ -1102,21 +1104,21 @@ __global__ void __launch_bounds__(256)
 
 __global__ void df_trmv_t_sum_kernel(const float* __restrict__ ph, const float* __restrict__ pl, int64_t S,
                                      int64_t nchunk, double* __restrict__ y, float* __restrict__ yh,
-                                     float* __restrict__ yl) {
+                                     float* __restrict__ yl, int add) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < S; i += (int64_t)gridDim.x * blockDim.x) {
         df tot = {0.f, 0.f};
         for (int64_t c = i / TRMV_ROWS; c < nchunk; ++c) tot = df_add(tot, {ph[c * S + i], pl[c * S + i]});
-        store_y(df_to(tot), i, y, yh, yl);
+        store_y(df_to(tot), i, y, yh, yl, add != 0);
     }
 }
 
-// y = A x, or y = b - A x when b is set, for a full double-float A (x as
-// planes; b, y float64, y also as planes when yh is set); one warp per row,
-// four independent accumulators per lane
+// y = A x, y = b - A x when b is set, or y += A x with add, for a full
+// double-float A (x as planes; b, y float64, y also as planes when yh is set);
+// one warp per row, four independent accumulators per lane
 __global__ void __launch_bounds__(256)
     df_gemv_kernel(const float* __restrict__ Ah, const float* __restrict__ Al, int64_t S,
                    const float* __restrict__ xh, const float* __restrict__ xl, const double* __restrict__ b,
-                   double* __restrict__ y, float* __restrict__ yh, float* __restrict__ yl) {
+                   double* __restrict__ y, float* __restrict__ yh, float* __restrict__ yl, int add) {
     const int lane = threadIdx.x & 31;
     const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (i >= S) return;
@@ -1129,12 +1131,7 @@ __global__ void __launch_bounds__(256)
         for (int u = 0; u < 4; ++u) df_fma_acc(acc[u], {rh[j + 32 * u], rl[j + 32 * u]}, {xh[j + 32 * u], xl[j + 32 * u]});
     for (; j < S; j += 32) df_fma_acc(acc[0], {rh[j], rl[j]}, {xh[j], xl[j]});
     const double v = warp_sum(df_to(df_add(df_add(acc[0], acc[1]), df_add(acc[2], acc[3]))));
-    if (lane == 0) store_y(b ? b[i] - v : v, i, y, yh, yl);
-}
-
-__global__ void add_vec_kernel(double* __restrict__ x, const double* __restrict__ d, int64_t n) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
-        x[t] += d[t];
+    if (lane == 0) store_y(b ? b[i] - v : v, i, y, yh, yl, add != 0);
 }
 
 // partial sums of squares of a lower-triangular double-float matrix
@@ -1436,17 +1433,15 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
     return AIh ? df_mirror_lower(AIh, AIl, S, st) : AJ_OK;
 }
 
-// x = A^-1 b = Li^T (Li b) with the inverse factor, b and x may alias.  The
-// scratch vectors hold b's and Li b's planes (S hi floats, then S lo floats).
+// x = Li^T (Li b) with the inverse factor, b given as planes bh (S hi floats,
+// then S lo floats); uh is 2 S floats of scratch.  x's planes go to xh/xl when
+// xh is set; with add, the product is added to x instead of replacing it.
 // (Two triangular products split the conditioning between two factors of
 // sqrt(cond A); one product with an explicit A^-1 would lose cond(A) at once.)
-int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_t st) {
+static int df_trsolve(int64_t S, DfSpd& w, const float* bh, float* uh, double* x, float* xh, float* xl, bool add,
+                      cudaStream_t st) {
     if (!w.Ih) return AJ_ERR_ARG;
-    float* bh = reinterpret_cast<float*>(w.vec);
-    float* uh = reinterpret_cast<float*>(w.vec2);
-    AJ_TRY(df_split(b, S, bh, bh + S, st));
-    const unsigned g = blocks_for(S * 32, 256);
-    df_trmv_kernel<<<g, 256, 0, st>>>(w.Ih, w.Il, S, bh, bh + S, nullptr, uh, uh + S);
+    df_trmv_kernel<<<blocks_for(S * 32, 256), 256, 0, st>>>(w.Ih, w.Il, S, bh, bh + S, nullptr, uh, uh + S);
     AJ_LAUNCHED();
     const int64_t nchunk = (S + TRMV_ROWS - 1) / TRMV_ROWS;
     float* ph = w.part;
@@ -1454,32 +1449,33 @@ int dfspd_solve_vec(int64_t S, DfSpd& w, const double* b, double* x, cudaStream_
     df_trmv_t_part_kernel<<<dim3((unsigned)((S + 31) / 32), (unsigned)nchunk), 256, 0, st>>>(w.Ih, w.Il, S, uh,
                                                                                            uh + S, ph, pl);
     AJ_LAUNCHED();
-    df_trmv_t_sum_kernel<<<blocks_for(S, 256, 64), 256, 0, st>>>(ph, pl, S, nchunk, x, nullptr, nullptr);
+    df_trmv_t_sum_kernel<<<blocks_for(S, 256, 64), 256, 0, st>>>(ph, pl, S, nchunk, x, xh, xl, add ? 1 : 0);
     return check_launch();
 }
 
-// x = A^-1 b with one step of iterative refinement against A (planes); r is S
-// scratch.  The correction A^-1 r goes through A^-1's planes (one row-wise
-// product) when they are given: r is already small, so the explicit inverse's
-// cond(A) loss applies to a correction, not to the solution.
-int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x, double* r,
-                        cudaStream_t st, const float* AIh, const float* AIl) {
-    AJ_TRY(dfspd_solve_vec(S, w, b, x, st));
+// x = A^-1 b with one step of iterative refinement against A (planes).  The
+// correction A^-1 r goes through A^-1's planes (one row-wise product) when
+// they are given: r is already small, so the explicit inverse's cond(A) loss
+// applies to a correction, not to the solution.  Five launches: each product
+// also writes the planes the next one reads, the residual never exists in
+// float64, and the last product adds the correction to x in place.
+// b_split: b's planes are already in w.vec (S hi floats, then S lo floats).
+// xh/xl, when set, receive the planes of the final x.
+int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x,
+                        cudaStream_t st, const float* AIh, const float* AIl, bool b_split, float* xh, float* xl) {
+    if (!w.Ih) return AJ_ERR_ARG;
+    float* v1 = reinterpret_cast<float*>(w.vec);   // b's planes, then x0's
+    float* v2 = reinterpret_cast<float*>(w.vec2);  // L^-1 b's planes, then r's
+    if (!b_split) AJ_TRY(df_split(b, S, v1, v1 + S, st));
+    AJ_TRY(df_trsolve(S, w, v1, v2, x, v1, v1 + S, false, st));
     const unsigned g = blocks_for(S * 32, 256);
-    float* xh = reinterpret_cast<float*>(w.vec);
-    AJ_TRY(df_split(x, S, xh, xh + S, st));
-    df_gemv_kernel<<<g, 256, 0, st>>>(Ah, Al, S, xh, xh + S, b, r, nullptr, nullptr);
+    df_gemv_kernel<<<g, 256, 0, st>>>(Ah, Al, S, v1, v1 + S, b, nullptr, v2, v2 + S, 0);
     AJ_LAUNCHED();
     if (AIh) {
-        float* rh = reinterpret_cast<float*>(w.vec2);
-        AJ_TRY(df_split(r, S, rh, rh + S, st));
-        df_gemv_kernel<<<g, 256, 0, st>>>(AIh, AIl, S, rh, rh + S, nullptr, r, nullptr, nullptr);
-        AJ_LAUNCHED();
-    } else {
-        AJ_TRY(dfspd_solve_vec(S, w, r, r, st));
+        df_gemv_kernel<<<g, 256, 0, st>>>(AIh, AIl, S, v2, v2 + S, nullptr, x, xh, xl, 1);
+        return check_launch();
     }
-    add_vec_kernel<<<blocks_for(S, 256, 64), 256, 0, st>>>(x, r, S);
-    return check_launch();
+    return df_trsolve(S, w, v2, v1, x, xh, xl, true, st);
 }
 
 int df_frob_lower(const float* h, const float* l, int64_t S, double* partial, int64_t nparts, cudaStream_t st) {
