@@ -45,6 +45,12 @@ inline unsigned blocks_for(int64_t n, int threads, int64_t cap = (1ll << 31) - 1
 
 inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 
+// true when every pointer is 16-byte aligned (for float4 loads)
+template <typename... T>
+inline bool aligned16(const T*... p) {
+    return ((reinterpret_cast<uintptr_t>(p) % 16 == 0) && ...);
+}
+
 // Carves typed sub-buffers out of a caller workspace.
 struct Carver {
     char* base;

@@ -181,49 +181,124 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Which terms of the weight gradient mapping entry b of a row takes (dense-mapping semantics: a
+// later duplicate of the same source pixel overwrites an earlier one, and the row ends at -1).
+// Returns false when the entry contributes nothing.
+__device__ __forceinline__ bool wg_entry(const int64_t* row, int64_t B, int64_t b, int64_t S, int compact_mode,
+                                         int64_t& sp, bool& keepD, bool& keepF) {
+    for (int64_t q = 0; q <= b; ++q)
+        if (row[q] == -1) return false;
+    sp = row[b];
+    if (sp < 0 || sp >= S) return false;
+    bool last = true;
+    for (int64_t q = b + 1; q < B; ++q) {
+        if (row[q] == -1) break;
+        if (row[q] == sp) last = false;
+    }
+    keepD = last;
+    keepF = compact_mode ? true : last;
+    return true;
+}
+
 // The same gradient on the mixed path, from the double-float planes of Omega
 // (M x S) and A^-1 (S x S) and of s: the dot products run as double-float on
-// the float32 pipe, with no float64 copies of Omega or A^-1.
-__global__ void __launch_bounds__(256)
+// the float32 pipe, with no float64 copies of Omega or A^-1.  One block per
+// image pixel m: each thread reads its slices of Omega's row once and forms
+// Omega_m . s and up to kWgDots products Omega_m . A^-1_sp side by side (16-byte
+// loads when every row is 16-byte aligned), so a thread's dependent chain is
+// S / kWgThreads steps long; a block reduction in fixed order finishes them.
+constexpr int kWgThreads = 128;
+constexpr int kWgDots = 4;
+
+__global__ void __launch_bounds__(kWgThreads)
     weight_grad_df_kernel(const int64_t* __restrict__ idx, int64_t M, int64_t B, int64_t S,
                           const float* __restrict__ Omh, const float* __restrict__ Oml, const float* __restrict__ AIh,
                           const float* __restrict__ AIl, const float* __restrict__ sh, const float* __restrict__ sl,
-                          const double* __restrict__ s, const double* __restrict__ dirty, int compact_mode,
+                          const double* __restrict__ s, const double* __restrict__ dirty, int compact_mode, int vec4,
                           double* __restrict__ grad) {
-    const int lane = threadIdx.x & 31;
-    const int64_t m = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (m >= M) return;
+    __shared__ double red[kWgThreads / 32][1 + kWgDots];
+    __shared__ double tot[1 + kWgDots];
+    const int64_t m = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const float* oh = Omh + m * S;
     const float* ol = Oml + m * S;
-    df acc = {0.f, 0.f};
-    for (int64_t j = lane; j < S; j += 32) df_fma_acc(acc, {oh[j], ol[j]}, {sh[j], sl[j]});
-    const double oms = warp_sum(df_to(acc));
     const int64_t* row = idx + m * B;
-    bool ended = false;
-    for (int64_t b = 0; b < B; ++b) {
-        const int64_t sp = row[b];
-        if (sp == -1) ended = true;
-        double g = 0.0;
-        if (!ended && sp >= 0 && sp < S) {
-            bool last = true;  // not overwritten by a later entry (dense-mapping semantics)
-            for (int64_t q = b + 1; q < B; ++q) {
-                if (row[q] == -1) break;
-                if (row[q] == sp) last = false;
-            }
-            const bool keepD = last;
-            const bool keepF = compact_mode ? true : last;
-            double oa = 0.0;
-            if (keepF) {
-                const float* ah = AIh + sp * S;
-                const float* al = AIl + sp * S;
-                df a = {0.f, 0.f};
-                for (int64_t j = lane; j < S; j += 32) df_fma_acc(a, {oh[j], ol[j]}, {ah[j], al[j]});
-                oa = warp_sum(df_to(a));
-            }
-            if (keepD) g += dirty[m] * s[sp];
-            if (keepF) g -= oms * s[sp] + oa;
+    double oms = 0.0;
+    for (int64_t b0 = 0; b0 < B; b0 += kWgDots) {
+        const bool first = b0 == 0;
+        const float* ah[kWgDots];
+        const float* al[kWgDots];
+#pragma unroll
+        for (int u = 0; u < kWgDots; ++u) {
+            int64_t sp;
+            bool kd, kf;
+            const bool use = b0 + u < B && wg_entry(row, B, b0 + u, S, compact_mode, sp, kd, kf) && kf;
+            ah[u] = use ? AIh + sp * S : nullptr;
+            al[u] = use ? AIl + sp * S : nullptr;
         }
-        if (lane == 0) grad[m * B + b] = g;
+        df acc[1 + kWgDots];
+#pragma unroll
+        for (int u = 0; u <= kWgDots; ++u) acc[u] = {0.f, 0.f};
+        if (vec4) {
+            for (int64_t t = threadIdx.x; t < S / 4; t += kWgThreads) {
+                const float4 h = reinterpret_cast<const float4*>(oh)[t];
+                const float4 l = reinterpret_cast<const float4*>(ol)[t];
+                if (first) {
+                    const float4 xh = reinterpret_cast<const float4*>(sh)[t];
+                    const float4 xl = reinterpret_cast<const float4*>(sl)[t];
+                    df_fma_lazy(acc[0], {h.x, l.x}, {xh.x, xl.x});
+                    df_fma_lazy(acc[0], {h.y, l.y}, {xh.y, xl.y});
+                    df_fma_lazy(acc[0], {h.z, l.z}, {xh.z, xl.z});
+                    df_fma_lazy(acc[0], {h.w, l.w}, {xh.w, xl.w});
+                    df_renorm(acc[0]);
+                }
+#pragma unroll
+                for (int u = 0; u < kWgDots; ++u) {
+                    if (!ah[u]) continue;
+                    const float4 xh = reinterpret_cast<const float4*>(ah[u])[t];
+                    const float4 xl = reinterpret_cast<const float4*>(al[u])[t];
+                    df_fma_lazy(acc[1 + u], {h.x, l.x}, {xh.x, xl.x});
+                    df_fma_lazy(acc[1 + u], {h.y, l.y}, {xh.y, xl.y});
+                    df_fma_lazy(acc[1 + u], {h.z, l.z}, {xh.z, xl.z});
+                    df_fma_lazy(acc[1 + u], {h.w, l.w}, {xh.w, xl.w});
+                    df_renorm(acc[1 + u]);
+                }
+            }
+        } else {
+            for (int64_t t = threadIdx.x; t < S; t += kWgThreads) {
+                const df o = {oh[t], ol[t]};
+                if (first) df_fma_acc(acc[0], o, {sh[t], sl[t]});
+#pragma unroll
+                for (int u = 0; u < kWgDots; ++u)
+                    if (ah[u]) df_fma_acc(acc[1 + u], o, {ah[u][t], al[u][t]});
+            }
+        }
+        // block sums in a fixed order: lanes (warp_sum), then warps 0, 1, ...
+#pragma unroll
+        for (int u = 0; u <= kWgDots; ++u) {
+            const double v = warp_sum(df_to(acc[u]));
+            if (lane == 0) red[warp][u] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x <= kWgDots) {
+            double v = 0.0;
+            for (int w = 0; w < kWgThreads / 32; ++w) v += red[w][threadIdx.x];
+            tot[threadIdx.x] = v;
+        }
+        __syncthreads();
+        if (first) oms = tot[0];
+        if (threadIdx.x < kWgDots && b0 + threadIdx.x < B) {
+            const int64_t b = b0 + threadIdx.x;
+            int64_t sp;
+            bool keepD = false, keepF = false;
+            double g = 0.0;
+            if (wg_entry(row, B, b, S, compact_mode, sp, keepD, keepF)) {
+                if (keepD) g += dirty[m] * s[sp];
+                if (keepF) g -= oms * s[sp] + tot[1 + threadIdx.x];
+            }
+            grad[m * B + b] = g;
+        }
+        __syncthreads();  // red and tot are reused by the next pass
     }
 }
 
@@ -618,9 +693,10 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
     }
     if (M > 0 && B > 0) {
         if (mixed)
-            weight_grad_df_kernel<<<blocks_for(M * 32, 256), 256, 0, st>>>(
+            weight_grad_df_kernel<<<(unsigned)M, kWgThreads, 0, st>>>(
                 p->pix_indexes, M, B, S, b.Omh, b.Oml, b.AIh, b.AIl, b.sh, b.sl, b.s, p->dirty_image,
-                b.compact ? 1 : 0, grad_weights);
+                b.compact ? 1 : 0,
+                S % 4 == 0 && aligned16(b.Omh, b.Oml, b.AIh, b.AIl, b.sh, b.sl) ? 1 : 0, grad_weights);
         else
             weight_grad_kernel<<<blocks_for(M * 32, 256), 256, 0, st>>>(p->pix_indexes, M, B, S, b.Om, b.Ainv, b.s,
                                                                         p->dirty_image, b.compact ? 1 : 0,

@@ -207,6 +207,54 @@ def test_mixed_matches_fp64_at_multi_chunk_sizes(aj, config, K):
         assert abs(out["mixed"][0] - out["fp64"][0]) <= 1e-7 * abs(out["fp64"][0]), (lam, out)
 
 
+def test_mixed_weight_gradient_ragged_rows(aj):
+    """S = 101 (Omega's and A^-1's rows are not 16-byte aligned, so the gradient takes its scalar
+    loads) and mapping rows padded to B = 7: later repeats that overwrite earlier entries, entries
+    after an early -1, and rows with more live entries than one pass of the per-pixel products takes."""
+    import torch
+
+    from autojax_gb300 import synthetic
+
+    cfg = synthetic.Config("ragged", 500, 30, 0.1, 1.2, 101, "delaunay", 0.8, 1.5, 1.0, 11)
+    d = synthetic.make_dataset(cfg)
+    S = d["S"]
+    assert S % 4 != 0
+    dev = torch.device("cuda")
+    wc = aj.w_compact_curvature_interferometer_from(d["grid_size"], torch.from_numpy(d["noise_map_real"]).to(dev),
+                                                    torch.from_numpy(d["uv_wavelengths"]).to(dev), d["pixel_scale"])
+    W = aj.w_tilde_via_compact_from(wc, torch.from_numpy(d["native_index_for_slim_index"]).to(dev)).cpu().numpy()
+    idx3, w3 = d["pix_indexes_for_sub_slim_index"], d["pix_weights_for_sub_slim_index"]
+    M = idx3.shape[0]
+    rng = np.random.default_rng(5)
+    idx = np.full((M, 7), -1, np.int64)
+    wts = np.zeros((M, 7))
+    idx[:, :3], wts[:, :3] = idx3, w3
+    for m in range(M):
+        kind = m % 4
+        if kind == 1:  # a repeat overwrites the earlier entry
+            idx[m, 3:5] = [idx3[m, 0], rng.integers(S)]
+            wts[m, 3:5] = rng.uniform(0.05, 0.5, 2)
+        elif kind == 2:  # entries after an early -1 are ignored
+            idx[m, 4:6] = rng.integers(S, size=2)
+            wts[m, 4:6] = 0.4
+        elif kind == 3:  # six live entries: a second pass of the dot products
+            idx[m, 3:6] = [rng.integers(S), idx3[m, 1], rng.integers(S)]
+            wts[m, 3:6] = rng.uniform(0.05, 0.3, 3)
+    args = (d["dirty_image"], d["data"], d["noise_map"], W, idx, wts, d["neighbors"], d["neighbors_sizes"])
+    coef = 0.5
+    logE, dlam, gw = aj.log_evidence_and_grad(*args, coefficient=coef, precision="mixed")
+    r_logE, r_dlam, r_gw = adjoint.log_evidence_and_grad(*args, coefficient=coef)
+    assert abs(logE - r_logE) <= 1e-8 * abs(r_logE), (logE, r_logE)
+    from oracle import numpy_port as ref
+
+    T = ref.mapping_matrix_from(idx, wts, S)
+    ev = np.linalg.eigvalsh(T.T @ W @ T + ref.constant_regularization_matrix_from(coef, d["neighbors"],
+                                                                                   d["neighbors_sizes"]))
+    cond = ev[-1] / ev[0]
+    assert np.all(gw[idx == -1] == 0) and np.all(gw[:, 3:][(np.arange(M) % 4 == 2)] == 0)
+    np.testing.assert_allclose(gw, r_gw, rtol=0, atol=max(1e-5, 2e-15 * cond) * np.abs(r_gw).max())
+
+
 def test_tile_policy_does_not_change_results():
     """The 64 x 64 and 32 x 32 tile kernels add in the same order: any tile policy gives the same bits."""
     import torch
