@@ -592,6 +592,8 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
             DfSpd* hw[1] = {&b.dh};
             double* hld[1] = {b.logdets + 1};
             rc = dfspd_factor_invert_n(hh, hl, 1, with_grad ? 1 : 0, S, hw, hld, info, hlane, nullptr, nullptr, true);
+            // tr(H^-1)'s partial sums for dlogE/dlambda here too, long before the evaluation's tail
+            if (rc == AJ_OK && with_grad) rc = df_frob_lower(b.dh.Ih, b.dh.Il, S, b.fpart, b.nfrob, hlane);
             if (cudaEventRecord(ln.ev[kEvHDone], hlane) != cudaSuccess) return AJ_ERR_CUDA;
             if (rc != AJ_OK) {
                 cudaStreamWaitEvent(st, ln.ev[kEvHDone], 0);
@@ -656,10 +658,14 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         if (cudaStreamWaitEvent(st, ln.ev[kEvHDone], 0) != cudaSuccess) return AJ_ERR_CUDA;
     }
 
-    // logE from the chi^2 and log-noise sums (side lane), s.D and the log-determinants
-    assemble_kernel<<<1, 1024, 0, st>>>(b.kpart, b.nk_blocks, K, b.s, b.D, S, b.logdets, mixed ? b.logdets + 4 : nullptr,
-                                        out);
-    AJ_LAUNCHED();
+    // logE from the chi^2 and log-noise sums (side lane), s.D and the log-determinants; on the
+    // mixed path with the gradient it runs on the side lane beside the weight gradient
+    const bool side_assemble = mixed && with_grad;
+    if (!side_assemble) {
+        assemble_kernel<<<1, 1024, 0, st>>>(b.kpart, b.nk_blocks, K, b.s, b.D, S, b.logdets,
+                                            mixed ? b.logdets + 4 : nullptr, out);
+        AJ_LAUNCHED();
+    }
     if (reconstruction &&
         cudaMemcpyAsync(reconstruction, b.s, sizeof(double) * S, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
         return AJ_ERR_CUDA;
@@ -673,12 +679,16 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         frob_lower_kernel<<<(unsigned)b.nfrob, 256, 0, st>>>(b.wh.Linv, S, b.fpart);
         AJ_LAUNCHED();
     }
-    // dlogE/dlambda (and, mixed, tr(H^-1)'s partial sums) on the side lane while st computes
-    // the weight gradient; both read only finished data
+    // dlogE/dlambda (and, mixed, the assembly) on the side lane while st computes the weight
+    // gradient; both read only finished data
     if (cudaEventRecord(ln.ev[kEvPre], st) != cudaSuccess || cudaStreamWaitEvent(pre, ln.ev[kEvPre], 0) != cudaSuccess)
         return AJ_ERR_CUDA;
     {
-        int rc = mixed ? df_frob_lower(b.dh.Ih, b.dh.Il, S, b.fpart, b.nfrob, pre) : AJ_OK;
+        int rc = AJ_OK;
+        if (side_assemble) {
+            assemble_kernel<<<1, 1024, 0, pre>>>(b.kpart, b.nk_blocks, K, b.s, b.D, S, b.logdets, b.logdets + 4, out);
+            rc = check_launch();
+        }
         if (rc == AJ_OK) {
             dlam_kernel<<<1, 1024, 0, pre>>>(p->neighbors, p->neighbors_sizes, S, p->P, b.s, mixed ? nullptr : b.Ainv,
                                              b.AIh, b.AIl, b.fpart, b.nfrob, p->coefficient, p->coefficient_dev,
