@@ -119,17 +119,28 @@ class LogEvidence:
         self.with_grad = bool(with_grad)
         self.M, self.K = ds.M, ds.K
         self.S, self.B, self.P = int(S), int(B), int(P)
-        # persistent per-model inputs (graph replays read these addresses)
-        self.pix_indexes = torch.zeros((self.M, self.B), dtype=torch.int64, device=dev)
-        self.pix_weights = torch.zeros((self.M, self.B), dtype=torch.float64, device=dev)
-        self.neighbors = torch.full((self.S, self.P), -1, dtype=torch.int64, device=dev)
-        self.neighbors_sizes = torch.zeros(self.S, dtype=torch.int64, device=dev)
-        self.coefficient = torch.ones(1, dtype=torch.float64, device=dev)
-        # outputs
-        self.out = torch.zeros(2, dtype=torch.float64, device=dev)
-        self.grad_weights = torch.zeros((self.M, self.B), dtype=torch.float64, device=dev)
+        # persistent per-model inputs (graph replays read these addresses), views of one buffer of
+        # 8-byte slots so an end-to-end call moves them with one copy; each starts 16-byte aligned
+        M, B, S, P = self.M, self.B, self.S, self.P
+        seg = {}
+        n_in = 0
+        for name, n in (("idx", M * B), ("w", M * B), ("nb", S * P), ("nsz", S), ("coef", 1)):
+            seg[name] = slice(n_in, n_in + n)
+            n_in += n + (n & 1)
+        self._in = torch.zeros(n_in, dtype=torch.int64, device=dev)
+        self.pix_indexes = self._in[seg["idx"]].view(M, B)
+        self.pix_weights = self._in[seg["w"]].view(torch.float64).view(M, B)
+        self.neighbors = self._in[seg["nb"]].view(S, P)
+        self.neighbors_sizes = self._in[seg["nsz"]]
+        self.coefficient = self._in[seg["coef"]].view(torch.float64)
+        self.neighbors.fill_(-1)
+        self.coefficient.fill_(1.0)
+        # outputs, packed likewise: logE and dlogE/dlambda, the info word (two int32), the gradient
+        self._outbuf = torch.zeros(4 + M * B, dtype=torch.float64, device=dev)
+        self.out = self._outbuf[0:2]
+        self.info = self._outbuf[2:3].view(torch.int32)
+        self.grad_weights = self._outbuf[4:].view(M, B)
         self.reconstruction = torch.zeros(self.S, dtype=torch.float64, device=dev)
-        self.info = torch.zeros(2, dtype=torch.int32, device=dev)
         self.problem = self._problem()
         nbytes = self.lib.aj_log_evidence_workspace_size(self.problem, self.pc, int(self.with_grad))
         if nbytes == 0:
@@ -137,14 +148,15 @@ class LogEvidence:
         self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=dev)
         self.graph = None
         self.launches_per_eval = None
-        # pinned staging for host inputs/outputs (end-to-end calls)
-        self._h_idx = torch.empty((self.M, self.B), dtype=torch.int64).pin_memory()
-        self._h_w = torch.empty((self.M, self.B), dtype=torch.float64).pin_memory()
-        self._h_nb = torch.empty((self.S, self.P), dtype=torch.int64).pin_memory()
-        self._h_nsz = torch.empty(self.S, dtype=torch.int64).pin_memory()
-        self._h_coef = torch.empty(1, dtype=torch.float64).pin_memory()
-        self._h_out = torch.empty(2, dtype=torch.float64).pin_memory()
-        self._h_grad = torch.empty((self.M, self.B), dtype=torch.float64).pin_memory()
+        # pinned staging for host inputs/outputs (end-to-end calls), laid out like the device buffers
+        self._h_in = torch.zeros(n_in, dtype=torch.int64).pin_memory()
+        self._h_outbuf = torch.zeros(4 + M * B, dtype=torch.float64).pin_memory()
+        hi = self._h_in.numpy()
+        self._h_idx = hi[seg["idx"]].reshape(M, B)
+        self._h_w = hi[seg["w"]].view(np.float64).reshape(M, B)
+        self._h_nb = hi[seg["nb"]].reshape(S, P)
+        self._h_nsz = hi[seg["nsz"]]
+        self._h_coef = hi[seg["coef"]].view(np.float64)
 
     def _problem(self) -> _lib.Problem:
         p = _lib.Problem()
@@ -240,6 +252,10 @@ class LogEvidence:
 
     def check(self):
         code, where = (int(v) for v in self.info.tolist())
+        self._raise_info(code, where)
+
+    @staticmethod
+    def _raise_info(code: int, where: int):
         if code == _lib.AJ_INFO_NOT_POSITIVE_DEFINITE:
             raise np.linalg.LinAlgError(f"curvature_reg_matrix is not positive definite (pivot {where})")
         if code == _lib.AJ_INFO_INDEX_RANGE:
@@ -253,32 +269,31 @@ class LogEvidence:
 
         Returns (logE, dlogE/dlambda, dlogE/dpix_weights) as NumPy values.
         """
-        self._h_idx.numpy()[...] = pix_indexes
-        self._h_w.numpy()[...] = pix_weights
+        self._h_idx[...] = pix_indexes
+        self._h_w[...] = pix_weights
         nb = np.asarray(neighbors)
-        self._h_nb.numpy()[...] = -1
-        self._h_nb.numpy()[:, : nb.shape[1]] = nb
-        self._h_nsz.numpy()[...] = neighbors_sizes
-        self._h_coef.numpy()[0] = coefficient
-        self.pix_indexes.copy_(self._h_idx, non_blocking=True)
-        self.pix_weights.copy_(self._h_w, non_blocking=True)
-        self.neighbors.copy_(self._h_nb, non_blocking=True)
-        self.neighbors_sizes.copy_(self._h_nsz, non_blocking=True)
-        self.coefficient.copy_(self._h_coef, non_blocking=True)
+        self._h_nb[...] = -1
+        self._h_nb[:, : nb.shape[1]] = nb
+        self._h_nsz[...] = neighbors_sizes
+        self._h_coef[0] = coefficient
+        self._in.copy_(self._h_in, non_blocking=True)
         self.step()
-        self._h_out.copy_(self.out, non_blocking=True)
-        if self.with_grad:
-            self._h_grad.copy_(self.grad_weights, non_blocking=True)
+        n_out = self._n_out()
+        self._h_outbuf[:n_out].copy_(self._outbuf[:n_out], non_blocking=True)
         torch.cuda.current_stream(self.device).synchronize()
-        self.check()
-        o = self._h_out.numpy()
-        return float(o[0]), float(o[1]), (self._h_grad.numpy().copy() if self.with_grad else None)
+        o = self._h_outbuf.numpy()
+        code, where = (int(v) for v in o[2:3].view(np.int32))
+        self._raise_info(code, where)
+        return float(o[0]), float(o[1]), (o[4:n_out].reshape(self.M, self.B).copy() if self.with_grad else None)
+
+    def _n_out(self) -> int:
+        return self._outbuf.numel() if self.with_grad else 4
 
     def h2d_bytes(self) -> int:
-        return sum(t.numel() * t.element_size() for t in (self._h_idx, self._h_w, self._h_nb, self._h_nsz, self._h_coef))
+        return self._h_in.numel() * 8
 
     def d2h_bytes(self) -> int:
-        return self._h_out.numel() * 8 + (self._h_grad.numel() * 8 if self.with_grad else 0)
+        return self._n_out() * 8
 
 
 class LogEvidenceBatch:

@@ -78,6 +78,28 @@ def test_evaluator_graph_replay_matches_direct(aj):
     assert ev.launches_per_eval and ev.launches_per_eval > 10
 
 
+def test_evaluate_host_reports_bad_index_then_recovers(aj):
+    """The end-to-end call reads the info word from its one device-to-host copy: an out-of-range
+    mapping index raises IndexError, and the next good call through the same graph is exact."""
+    from autojax_gb300.inversion import LogEvidence
+
+    d = gu.full_inputs("cfg1")
+    a = _args(d)
+    ev = LogEvidence(a[0], a[1], a[2], a[3], S=d["pixels"], B=a[4].shape[1], P=a[6].shape[1], precision="mixed")
+    ev.set_model(a[4], a[5], a[6], a[7], coefficient=0.7)
+    ev.capture()
+    bad = a[4].copy()
+    bad[3, 1] = d["pixels"]
+    with pytest.raises(IndexError, match=str(3 * a[4].shape[1] + 1)):
+        ev.evaluate_host(bad, a[5], a[6], a[7], 0.7)
+    logE, dlam, gw = ev.evaluate_host(a[4], a[5], a[6], a[7], 0.7)
+    r = adjoint.log_evidence_and_grad(*a, coefficient=0.7)
+    assert abs(logE - r[0]) <= 1e-8 * abs(r[0])
+    assert gw.shape == a[4].shape
+    assert ev.h2d_bytes() >= (a[4].size * 2 + a[6].size + d["pixels"] + 1) * 8
+    assert ev.d2h_bytes() == (4 + a[4].size) * 8
+
+
 def test_autograd_function(aj):
     import torch
 
