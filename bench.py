@@ -251,7 +251,7 @@ def time_region(fn, steps: int, dist: Dist, name: str = "region") -> float:
 ROOFLINE_TRAFFIC_BYTES = 72.9e6
 
 
-def roofline(A, dist: Dist):
+def roofline(A, dist: Dist, tune_policy: bool = True):
     """Roofline of the dominant kernel group of the mixed path: the double-float
     factorisation chain (Cholesky panel, trailing updates, triangular inverse,
     L^-T L^-1), run standalone through aj_spd_inverse_mixed on the S x S matrix
@@ -290,8 +290,18 @@ def roofline(A, dist: Dist):
     torch.cuda.synchronize()
     if int(info[0]) != 0:
         raise RuntimeError(f"roofline matrix not positive definite (info {info.tolist()})")
+    # the group alone shares the GPU differently from a whole evaluation (no H factorisation, no
+    # gathers beside it): time it with the tile policy tuned for this call, then restore the
+    # evaluation's
+    from autojax_gb300 import tune
+
+    saved = tune.get_tile_policy()
+    policy = tune.tune_tile_policy(lambda: inv_mixed(0), reps=3)["policy"] if tune_policy else saved
     reps = 5
-    t_inv_mixed = time_region(inv_mixed, reps, dist, "roofline_mixed") / reps
+    try:
+        t_inv_mixed = time_region(inv_mixed, reps, dist, "roofline_mixed") / reps
+    finally:
+        tune.set_tile_policy(*saved)
     t_inv_fp64 = time_region(inv_fp64, reps, dist, "roofline_fp64") / reps
     fp64_peak = fma_peak_tflops(_lib.AJ_FP64)
     fp32_peak = fma_peak_tflops(_lib.AJ_MIXED)
@@ -310,6 +320,7 @@ def roofline(A, dist: Dist):
                        "per double-float multiply-add",
         "traffic": ROOFLINE_TRAFFIC_BYTES,
         "S": S,
+        "tile_policy": list(policy),
         "ms": 1e3 * t_inv_mixed,
         "fp64_same_work_ms": 1e3 * t_inv_fp64,
         "fp64_same_work_frac_of_fp64_peak": inv_flops / t_inv_fp64 / 1e12 / fp64_peak,
@@ -331,7 +342,7 @@ def roofline_only(args, dist: Dist) -> dict:
     rng = np.random.default_rng(3)
     X = rng.standard_normal((S, S))
     A = torch.from_numpy(X @ X.T / S + np.eye(S)).cuda()
-    roof, fp64_peak, fp32_peak = roofline(A, dist)
+    roof, fp64_peak, fp32_peak = roofline(A, dist, tune_policy=False)
     return {"roofline": roof, "peaks": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak}}
 
 
@@ -425,7 +436,7 @@ def gpu_arm(args, dist: Dist) -> dict:
         w_tilde, torch.from_numpy(d["pix_indexes_for_sub_slim_index"]).to(dev),
         torch.from_numpy(d["pix_weights_for_sub_slim_index"]).to(dev), S)
     A = (A + F).contiguous()
-    roof, fp64_peak, fp32_peak = roofline(A, dist)
+    roof, fp64_peak, fp32_peak = roofline(A, dist, tune_policy=not args.tile_policy)
     del F
 
     result = {
