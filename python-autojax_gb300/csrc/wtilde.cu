@@ -32,7 +32,6 @@
 namespace aj {
 
 constexpr int PANEL_ROW_PAD = 128;  // panel columns (pixels) padded to the tile size
-constexpr int SLAB = 8;             // k-rows staged per shared-memory slab (f32 tiles)
 constexpr int FOLD = 256;           // k-rows summed in registers before a Kahan fold
 constexpr size_t PANEL_BUDGET = size_t(1) << 30;  // bytes of panel per K chunk
 
@@ -451,7 +450,8 @@ struct WtildePlan {
     size_t elem;
 };
 
-WtildePlan wtilde_plan(int64_t K, int64_t M, int precision) {
+// (both precisions store 8 bytes a panel element: a float64, or a hi + lo pair of float32)
+WtildePlan wtilde_plan(int64_t K, int64_t M) {
     WtildePlan p;
     p.Mp = pad_to(M > 0 ? M : 1, PANEL_ROW_PAD);
     p.elem = 8;  // float64, or a hi + lo pair of float32
@@ -530,7 +530,7 @@ using namespace aj;
 extern "C" {
 
 size_t aj_w_tilde_curvature_workspace_size(int64_t K, int64_t M, int precision) {
-    WtildePlan p = wtilde_plan(K, M, precision);
+    WtildePlan p = wtilde_plan(K, M);
     size_t panel = 2 * p.kc * p.Mp * p.elem;
     // the mixed path may join its double-float planes through this buffer
     if (precision == AJ_MIXED && panel < sizeof(double) * M * M) panel = sizeof(double) * M * M;
@@ -554,7 +554,7 @@ int aj_w_tilde_curvature(const double* noise_map_real, const double* uv, const d
             return AJ_ERR_CUDA;
         return AJ_OK;
     }
-    WtildePlan p = wtilde_plan(K, M, precision);
+    WtildePlan p = wtilde_plan(K, M);
     if (workspace_bytes < aj_w_tilde_curvature_workspace_size(K, M, precision) || !workspace) return AJ_ERR_WORKSPACE;
     if (precision == AJ_MIXED) {
         // the double-float result accumulates in planes: the caller's, else the float64 output's bytes
