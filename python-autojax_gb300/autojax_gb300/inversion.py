@@ -90,6 +90,19 @@ class Dataset:
             p.N = self.w_compact.shape[0]
 
 
+def staging_layout(M: int, B: int, S: int, P: int) -> tuple[dict, int]:
+    """Slices of one model's inputs in the buffer of 8-byte slots that an end-to-end call copies at
+    once: mapping indexes and weights (M x B), neighbours (S x P), neighbour counts (S) and the
+    regularisation coefficient (1).  Each segment starts on a 16-byte boundary.  Returns the
+    slices by name ("idx", "w", "nb", "nsz", "coef") and the buffer's length in slots."""
+    seg = {}
+    n = 0
+    for name, size in (("idx", M * B), ("w", M * B), ("nb", S * P), ("nsz", S), ("coef", 1)):
+        seg[name] = slice(n, n + size)
+        n += size + (size & 1)
+    return seg, n
+
+
 class LogEvidence:
     """Resident-dataset evaluator of the log-evidence and its gradient.
 
@@ -120,13 +133,9 @@ class LogEvidence:
         self.M, self.K = ds.M, ds.K
         self.S, self.B, self.P = int(S), int(B), int(P)
         # persistent per-model inputs (graph replays read these addresses), views of one buffer of
-        # 8-byte slots so an end-to-end call moves them with one copy; each starts 16-byte aligned
+        # 8-byte slots so an end-to-end call moves them with one copy
         M, B, S, P = self.M, self.B, self.S, self.P
-        seg = {}
-        n_in = 0
-        for name, n in (("idx", M * B), ("w", M * B), ("nb", S * P), ("nsz", S), ("coef", 1)):
-            seg[name] = slice(n_in, n_in + n)
-            n_in += n + (n & 1)
+        seg, n_in = staging_layout(M, B, S, P)
         self._in = torch.zeros(n_in, dtype=torch.int64, device=dev)
         self.pix_indexes = self._in[seg["idx"]].view(M, B)
         self.pix_weights = self._in[seg["w"]].view(torch.float64).view(M, B)
