@@ -107,3 +107,13 @@ def test_numpy_dtype_is_checked_like_the_reference_signatures():
 
     with pytest.raises(TypeError):
         aj.mapping_matrix_from(np.zeros((2, 3), np.int32), np.zeros((2, 3)), 4)
+
+
+def test_missing_library_raises_without_fallback(tmp_path, monkeypatch):
+    """With the extension not built, the first call raises (there is no CPU path to fall back to)."""
+    from autojax_gb300 import _lib
+
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "libautojax_gb300.so"))
+    with pytest.raises(_lib.LibraryError, match="no CPU fallback"):
+        _lib.load()
