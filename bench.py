@@ -114,8 +114,7 @@ class ClockSampler:
         self.path = None
 
     def start(self):
-        out_dir = ROOT / "gpurun_out" if (ROOT / "gpurun_out").is_dir() else Path(tempfile.gettempdir())
-        self.path = out_dir / f"clocks_{os.getpid()}.csv"
+        self.path = Path(tempfile.gettempdir()) / f"aj_bench_clocks_{os.getpid()}.csv"
         try:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
@@ -245,9 +244,9 @@ def time_region(fn, steps: int, dist: Dist, name: str = "region") -> float:
 
 
 # DRAM bytes (read + write) of one aj_spd_inverse_mixed call at S = 1,500, summed
-# over its launches, from the warm-cache ncu capture in
-# profiles/spd_inverse_mixed_s1500_traffic.md (16.0 MB read, 56.9 MB written):
-# the group's working set, 7 double-float S x S planes (63 MB), stays in L2.
+# over its launches in a warm-cache ncu capture of one call (16.0 MB read,
+# 56.9 MB written): the group's working set, 7 double-float S x S planes
+# (63 MB), stays in L2.
 ROOFLINE_TRAFFIC_BYTES = 72.9e6
 
 
@@ -325,6 +324,14 @@ def roofline(A, dist: Dist, tune_policy: bool = True):
         "fp64_same_work_ms": 1e3 * t_inv_fp64,
         "fp64_same_work_frac_of_fp64_peak": inv_flops / t_inv_fp64 / 1e12 / fp64_peak,
     }
+    # the same launch against the measured peaks (neither bounds a float32-pipe group)
+    mp = measured_peaks()
+    roof["frac_vs_measured_peaks"] = {
+        "bf16_tflops_sustained": (achieved / mp["bf16_tflops_sustained"]) if mp.get("bf16_tflops_sustained") else None,
+        "hbm_gbs": (ROOFLINE_TRAFFIC_BYTES / t_inv_mixed / 1e9 / mp["hbm_gbs"]) if mp.get("hbm_gbs") else None,
+        "note": "achieved float64-class TFLOP/s over the sustained bf16 tensor peak, and the group's DRAM "
+                "traffic per call over the timed duration against the copy bandwidth (MEASURED_PEAKS.json)",
+    }
     return roof, fp64_peak, fp32_peak
 
 
@@ -396,6 +403,7 @@ def gpu_arm(args, dist: Dist) -> dict:
 
     # accuracy of the mixed path against the float64 path over the lambda schedule
     rel = []
+    mixed_vals = {"logE": [], "s": []}
     for c in coefs:
         vals = {}
         for prec, e in ev.items():
@@ -405,6 +413,8 @@ def gpu_arm(args, dist: Dist) -> dict:
             e.check()
             vals[prec] = e.out.cpu().numpy().copy()
         rel.append(abs(vals["mixed"][0] - vals["fp64"][0]) / abs(vals["fp64"][0]))
+        mixed_vals["logE"].append(float(vals["mixed"][0]))
+        mixed_vals["s"].append(ev["mixed"].reconstruction.cpu().numpy().copy())
 
     for e in ev.values():
         f = stepper(e)
@@ -450,7 +460,7 @@ def gpu_arm(args, dist: Dist) -> dict:
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
+        "dtype": "df32 (double-float) + f64",
         "data": "synthetic (seeded; shapes and distributions of the K=1e6 configuration)",
         "config": {
             "workload": f"{args.config}: K={K} visibilities, M={M} image pixels (100x100 at 0.04\", r=2.4\"), "
@@ -463,7 +473,10 @@ def gpu_arm(args, dist: Dist) -> dict:
                             "tuned_ms": tuned["ms"], "default_ms": tuned["ms_default"],
                             "candidates_timed": tuned["candidates_timed"]},
         },
-        "fp64_path": {"value": args.steps * dist.world / t_fp64, "ms_per_step": 1e3 * t_fp64 / args.steps},
+        "fp64_path": {"value": args.steps * dist.world / t_fp64, "ms_per_step": 1e3 * t_fp64 / args.steps,
+                      # five S^3/6 multiply-add passes (Cholesky of A and H, L^-1 of both, L^-T L^-1)
+                      "fp64_pipe_floor_ms": 1e3 * 5 * S**3 / 6 * 2 / (fp64_peak * 1e12),
+                      "mixed_over_fp64_pipe_floor": (5 * S**3 / 6 * 2 / (fp64_peak * 1e12)) / (t_mixed / args.steps)},
         "mixed_over_fp64": t_fp64 / t_mixed,
         "max_rel_dlogE_mixed_vs_fp64": max(rel),
         "e2e": {"value": args.steps * dist.world / t_e2e, "unit": "evals/s", "h2d_bytes_per_step": e.h2d_bytes(),
@@ -476,6 +489,10 @@ def gpu_arm(args, dist: Dist) -> dict:
     }
     if not args.skip_wtilde:
         result["w_tilde"] = wtilde_bench(d, dev, fp32_peak)
+    if dist.rank == 0 and dist.world == 1 and not args.skip_cpu:
+        # the checker, after every timed region
+        result["err_vs_oracle"] = oracle_errors(d, w_tilde, mixed_vals, result.get("w_tilde"))
+    result.get("w_tilde", {}).pop("sample", None)
     if args.stages:
         result["stages_ms"] = stage_times(d, w_tilde, dev, dist)
     if not args.skip_batch:
@@ -584,11 +601,16 @@ def wtilde_bench(d, dev, fp32_peak) -> dict:
     sec = e0.elapsed_time(e1) / 1e3
     terms = M * (M + 1) / 2 * Ks
     fp32_flops = terms * 2 * 11.4 * 2
+    rng = np.random.default_rng(17)
+    rows = np.repeat(np.array([0, M // 3, M // 2, M - 1]), 64)
+    cols = rng.integers(0, M, rows.size)
+    cols[::64] = rows[::64]
+    Wh = W.cpu().numpy()
     return {"precision": "mixed (float64 panel, double-float product)", "K_sample": Ks, "M": M, "seconds": sec,
             "terms_per_s": terms / sec, "fp32_pipe_frac": fp32_flops / sec / 1e12 / fp32_peak,
-            "fp32_pipe_frac_note": "double-float arithmetic only (22.8 float32 instructions per term); ncu measures "
-                                   "the product kernel's FMA pipe at 74.5% active "
-                                   "(profiles/w_tilde_mixed_m5024_full.md)"}
+            "fp32_pipe_frac_note": "double-float arithmetic only (22.8 float32 instructions per term)",
+            "sample": {"rows": rows, "cols": cols, "values": Wh[rows, cols],
+                       "noise": d["noise_map_real"][:Ks].copy(), "uv": d["uv_wavelengths"][:Ks].copy()}}
 
 
 def stage_times(d, w_tilde, dev, dist) -> dict:
@@ -613,12 +635,12 @@ def stage_times(d, w_tilde, dev, dist) -> dict:
 # -------------------------------------------------------------- CPU legs
 
 
-def cpu_eval_setup(d: dict, k_sample: int = 20000):
-    """w_tilde for the host arm from a visibility sample (its values do not change the per-evaluation cost)."""
+def cpu_eval_setup(d: dict):
+    """w_tilde for the host legs at the workload's full K: the offset table by the oracle's
+    separable host product (seconds on host cores), expanded as numba.py:238-255 does."""
     from oracle import numpy_port as ref
 
-    wc = ref.w_compact_curvature_interferometer_from(d["grid_size"], d["noise_map_real"][:k_sample],
-                                                     d["uv_wavelengths"][:k_sample], d["pixel_scale"])
+    wc = ref.w_compact_separable(d["grid_size"], d["noise_map_real"], d["uv_wavelengths"], d["pixel_scale"])
     return ref.w_tilde_via_compact_from(wc, d["native_index_for_slim_index"])
 
 
@@ -645,16 +667,113 @@ def cpu_baseline(d: dict, W, budget_s: float = 20.0) -> dict:
     n = max(1, min(20, int(budget_s / max(sec1, 1e-3))))
     sec, n = cpu_time(d, W, n)
     return {"value": n / sec, "unit": "evals/s", "cores": cores(), "kind": "port",
-            "sample": f"{n} logE+grad evaluations of the workload's shapes on the host (NumPy port of numba.py "
-                      "logE + closed-form adjoint; w_tilde from a 20000-visibility sample, chi^2 over all K)"}
+            "sample": f"{n} logE+grad evaluations of the workload (NumPy port of numba.py logE + closed-form "
+                      "adjoint; w_tilde at the workload's full K, as the GPU arm uses)"}
+
+
+def reference_module():
+    """The reference's own numba.py from baseline/_ref (placed by baseline/stage_reference.py),
+    or None.  Without numba on the host its functions run un-jitted through a pass-through shim
+    (jit returns the function, prange is range), i.e. as the reference's NumPy source."""
+    import types
+
+    ref_dir = ROOT / "baseline" / "_ref"
+    if not (ref_dir / "autojax" / "numba.py").exists():
+        return None, "baseline/_ref not staged"
+    try:
+        import numba  # noqa: F401
+
+        how = "Numba JIT"
+    except ImportError:
+        shim = types.ModuleType("numba")
+
+        def jit(*args, **kwargs):
+            if len(args) == 1 and callable(args[0]) and not kwargs:
+                return args[0]
+            return lambda f: f
+
+        shim.jit = shim.njit = jit
+        shim.prange = range
+        sys.modules["numba"] = shim
+        how = "numba absent: the reference's Numba source executed as NumPy, not JIT"
+    if str(ref_dir) not in sys.path:
+        sys.path.insert(0, str(ref_dir))
+    from autojax import numba as ref_numba
+
+    return ref_numba, how
+
+
+def reference_time(mod, d: dict, W, evals: int) -> tuple[float, int]:
+    """The reference's log_likelihood_function_via_w_tilde_from (numba.py:761-857), unmodified:
+    logE only (the reference has no gradient) with its hard-coded coefficient 1.0."""
+    args = (d["dirty_image"], d["data"], d["noise_map"], W, d["pix_indexes_for_sub_slim_index"],
+            d["pix_weights_for_sub_slim_index"], d["neighbors"], d["neighbors_sizes"])
+    t0 = time.perf_counter()
+    for _ in range(evals):
+        mod.log_likelihood_function_via_w_tilde_from(*args)
+    return time.perf_counter() - t0, evals
+
+
+def oracle_errors(d: dict, w_tilde_dev, lm: dict, wt: dict | None) -> dict:
+    """Errors of the mixed path against the oracle (the checker) on the workload: logE and s at
+    every lambda of the schedule and F, all given the GPU's float64 w_tilde; w_tilde from the
+    mixed direct build on its visibility sample against the oracle's sums on sampled entries."""
+    import torch
+
+    import autojax_gb300 as aj
+    from oracle import numpy_port as ref
+
+    W = w_tilde_dev.cpu().numpy()
+    T = ref.mapping_matrix_from(d["pix_indexes_for_sub_slim_index"], d["pix_weights_for_sub_slim_index"], d["S"])
+    F_ref = ref.curvature_matrix_via_w_tilde_from(W, T)
+    D_ref = ref.data_vector_from(T, d["dirty_image"])
+    dev = w_tilde_dev.device
+    F = aj.curvature_matrix_via_w_wilde_sparse_mapping_matrix_from(
+        w_tilde_dev, torch.from_numpy(d["pix_indexes_for_sub_slim_index"]).to(dev),
+        torch.from_numpy(d["pix_weights_for_sub_slim_index"]).to(dev), d["S"], precision="mixed").cpu().numpy()
+    out = {"F": {"max_abs_err_over_max_abs": float(np.abs(F - F_ref).max() / np.abs(F_ref).max())},
+           "logE": [], "s": []}
+    for lam, logE_mixed, s_mixed in zip(LAMBDAS, lm["logE"], lm["s"]):
+        H = ref.constant_regularization_matrix_from(float(np.sqrt(lam)), d["neighbors"], d["neighbors_sizes"])
+        r_logE = ref._evidence(d["noise_map"], d["data"], F_ref, H, D_ref)
+        A = F_ref + H
+        s_ref = np.linalg.solve(A, D_ref)
+        ev = np.linalg.eigvalsh(A)
+        out["logE"].append({"lambda": lam, "rel_err": abs(logE_mixed - r_logE) / abs(r_logE), "oracle": r_logE})
+        out["s"].append({"lambda": lam, "rel_err": float(np.linalg.norm(s_mixed - s_ref) / np.linalg.norm(s_ref)),
+                         "cond_A": float(ev[-1] / ev[0])})
+    if wt is not None and "sample" in wt:
+        smp = wt.pop("sample")
+        rows, cols = smp["rows"], smp["cols"]
+        exp = ref.w_tilde_entries(smp["noise"], smp["uv"], d["grid_radians_slim"], rows, cols)
+        scale = float(np.abs(exp[rows == cols]).max())
+        out["w_tilde"] = {"max_abs_err_over_scale": float(np.abs(smp["values"] - exp).max() / scale),
+                          "entries": int(rows.size), "K_sample": int(smp["uv"].shape[0]),
+                          "scale": "largest diagonal entry"}
+    out["checker"] = "oracle/numpy_port.py (NumPy/LAPACK restatement of numba.py), same inputs"
+    return out
 
 
 def reference_arm(args, dist: Dist) -> dict:
     d = dataset(args.config)
     W = cpu_eval_setup(d)
-    for _ in range(max(0, min(args.warmup, 1))):
-        cpu_time(d, W, 1)
-    sec, n = cpu_time(d, W, args.steps)
+    mod, how = reference_module()
+    # the port's logE + gradient beside the reference's own logE
+    sec_p, n_p = cpu_time(d, W, max(1, min(args.steps, 5)))
+    port = {"value": n_p / sec_p, "unit": "logE+grad evals/s", "kind": "port",
+            "sample": f"{n_p} evaluations: numba.py logE restated in NumPy + the closed-form adjoint"}
+    if mod is not None:
+        for _ in range(max(0, min(args.warmup, 1))):
+            reference_time(mod, d, W, 1)
+        sec, n = reference_time(mod, d, W, args.steps)
+        kind, what = "reference", (f"{n} calls of the reference's own log_likelihood_function_via_w_tilde_from "
+                                   f"(numba.py:761-857, logE only: the reference has no gradient; {how})")
+    else:
+        for _ in range(max(0, min(args.warmup, 1))):
+            cpu_time(d, W, 1)
+        sec, n = cpu_time(d, W, args.steps)
+        kind, what = "port", (f"{n} logE+grad evaluations of the NumPy port ({how}); numba.py logE restated in "
+                              "NumPy + the closed-form adjoint")
     v = n / sec
     return {
         "metric": METRIC,
@@ -670,11 +789,11 @@ def reference_arm(args, dist: Dist) -> dict:
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded; shapes and distributions of the K=1e6 configuration)",
-        "config": {"workload": f"{args.config}: K={d['K']}, M={d['M']}, S={d['S']}; host NumPy port of numba.py",
-                   "lambdas": list(LAMBDAS)},
-        "cpu_baseline": {"value": v, "unit": "evals/s", "cores": cores(), "kind": "port",
-                         "sample": f"{n} logE+grad evaluations (numba.py logE restated in NumPy + closed-form "
-                                   "adjoint); w_tilde from a 20000-visibility sample"},
+        "config": {"workload": f"{args.config}: K={d['K']}, M={d['M']}, S={d['S']}; w_tilde at the full K "
+                               "(float64, precomputed as in numba.py:814)",
+                   "lambdas": list(LAMBDAS), "same_config": True},
+        "cpu_baseline": {"value": v, "unit": "evals/s", "cores": cores(), "kind": kind, "sample": what},
+        "port_logE_grad": port,
         "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -696,6 +815,7 @@ def main():
             torch.cuda.set_device(dist.local)
             res = {"w_tilde": wtilde_bench(dataset(args.config), torch.device("cuda", dist.local),
                                            fma_peak_tflops(1))}
+            res["w_tilde"].pop("sample", None)
         else:
             res = gpu_arm(args, dist)
         if dist.rank == 0 and dist.world == 1 and not args.skip_cpu and not args.only:

@@ -174,6 +174,14 @@ int aj_curvature_w_tilde_sparse(const double* w_tilde, int64_t M, const int64_t*
                                 const double* pix_weights, int64_t B, int64_t S, double* out, void* workspace,
                                 size_t workspace_bytes, int* info, void* stream);
 
+/* numba.py:591-614 curvature_matrix_via_w_wilde_sparse_mapping_matrix_from in double-float:
+ * the two gathers the AJ_MIXED likelihood runs (Omega = (T^T W)^T, then F = T^T Omega) from
+ * W's double-float planes (hi, lo; see aj_split_f64), joined to float64 in out (S, S). */
+size_t aj_curvature_w_tilde_sparse_mixed_workspace_size(int64_t M, int64_t B, int64_t S);
+int aj_curvature_w_tilde_sparse_mixed(const float* w_tilde_hi, const float* w_tilde_lo, int64_t M,
+                                      const int64_t* pix_indexes, const double* pix_weights, int64_t B, int64_t S,
+                                      double* out, void* workspace, size_t workspace_bytes, int* info, void* stream);
+
 /* numba.py:500-549 _w_compact_matmul_sparse_mapping_matrix_from: out (M, S) = W T
  * with W gathered from the compact table (N, 2N-1) on the fly. */
 int aj_w_compact_matmul_sparse(const double* w_compact, int64_t N, const int64_t* native_index, int64_t M,
@@ -218,11 +226,14 @@ int aj_spd_solve(const double* data_vector, const double* A, int64_t S, double* 
  * code whose allocator belongs to someone else): no workspace argument, and no
  * cudaMalloc, cudaFree or allocating library call. No counterpart in the
  * reference. Scratch is one file-scope __device__ array sized for
- * S <= AJ_NOALLOC_SOLVE_MAX_S (about 8.3 MB, held by every GPU that loads the
- * library until the process exits); larger S returns AJ_ERR_TOO_LARGE. The
- * first call on a device looks up the array's device address
- * (cudaGetSymbolAddress), so make that first call before any stream capture.
- * All calls on a device share the array: calls whose GPU work overlaps race. */
+ * S <= AJ_NOALLOC_SOLVE_MAX_S (about 8.3 MB); larger S returns
+ * AJ_ERR_TOO_LARGE. The driver places the array when it loads the library's
+ * device code into a context, which under lazy module loading (the CUDA
+ * default) is this entry point's first call in each context: that first call
+ * can fail for lack of device memory, so make it early and before any stream
+ * capture. The array then stays until the context ends. `info` is required
+ * (NULL returns AJ_ERR_ARG): a non-positive-definite A is reported only there.
+ * All calls in a context share the array: calls whose GPU work overlaps race. */
 #define AJ_NOALLOC_SOLVE_MAX_S 1024
 int aj_spd_solve_noalloc(const double* data_vector, const double* A, int64_t S, double* out, int* info, void* stream);
 
@@ -253,8 +264,8 @@ int aj_split_f64(const double* x, int64_t n, float* hi, float* lo, void* stream)
 
 /* Dimensions and inputs of one log-evidence evaluation. The shared W (M, M)
  * is w_tilde64, and for AJ_MIXED also its double-float planes w_tilde_hi /
- * w_tilde_lo (split once with aj_split_f64; without them the mixed path splits
- * w_tilde64 on every call); for the compact variant w_compact (N, 2N-1) and
+ * w_tilde_lo (split once with aj_split_f64, 16-byte aligned; without them the mixed
+ * path splits w_tilde64 on every call); for the compact variant w_compact (N, 2N-1) and
  * native_index (M, 2) replace it. */
 typedef struct aj_problem {
     int64_t M, K, S, B, P, N;
@@ -333,6 +344,14 @@ int aj_bilinear_weights_vjp(const double* beta, int64_t M, int64_t n, double hal
 int aj_log_evidence_batched(const aj_problem* problems, int64_t n, int precision, int with_grad, double* out,
                             double* const* grad_weights, double* const* reconstruction, void* const* workspaces,
                             const size_t* workspace_bytes, int* info, void* stream);
+
+/* Frees the side streams and events the library created for `stream` on the
+ * current device (the factorisation lanes, and for batches the branch streams
+ * with their lanes); they are otherwise kept until the process exits, one set
+ * per caller stream. Call it when no work issued through `stream` is in
+ * flight or being captured; a later call on the stream creates a fresh set.
+ * No reference counterpart. */
+int aj_release_stream(void* stream);
 
 /* CUDA-graph capture of library calls (no reference counterpart: the
  * reference evaluates eagerly).  Everything enqueued on `stream` between

@@ -83,6 +83,8 @@ SIGNATURES = {
     "aj_sparse_workspace_size": (SZ, [I64, I64, I64, I64]),
     "aj_sparse_mapping_matrix_transpose_matmul": (INT, [P, I64, I64, P, P, I64, I64, P, P, SZ, P, P]),
     "aj_curvature_w_tilde_sparse": (INT, [P, I64, P, P, I64, I64, P, P, SZ, P, P]),
+    "aj_curvature_w_tilde_sparse_mixed_workspace_size": (SZ, [I64, I64, I64]),
+    "aj_curvature_w_tilde_sparse_mixed": (INT, [P, P, I64, P, P, I64, I64, P, P, SZ, P, P]),
     "aj_w_compact_matmul_sparse": (INT, [P, I64, P, I64, P, P, I64, I64, P, P, SZ, P, P]),
     "aj_curvature_w_compact_sparse": (INT, [P, I64, P, I64, P, P, I64, I64, P, P, SZ, P, P]),
     "aj_curvature_preload_original_workspace_size": (SZ, [I64, I64, I64]),
@@ -112,6 +114,7 @@ SIGNATURES = {
     "aj_bilinear_weights": (INT, [P, I64, I64, D, P, P, P]),
     "aj_bilinear_weights_vjp": (INT, [P, I64, I64, D, P, P, P]),
     "aj_log_evidence_batched": (INT, [C.POINTER(Problem), I64, INT, INT, P, P, P, P, P, P, P]),
+    "aj_release_stream": (INT, [P]),
     "aj_graph_begin": (INT, [P]),
     "aj_graph_end": (INT, [P, C.POINTER(P)]),
     "aj_graph_launch": (INT, [P, P]),

@@ -257,13 +257,31 @@ def sparse_mapping_matrix_transpose_matmul(matrix, pix_indexes_for_sub_slim_inde
 
 
 def curvature_matrix_via_w_wilde_sparse_mapping_matrix_from(w_tilde, pix_indexes_for_sub_slim_index,
-                                                            pix_weights_for_sub_slim_index, pixels):
-    """numba.py:591-614 (the reference's public name keeps its 'wilde' spelling)."""
+                                                            pix_weights_for_sub_slim_index, pixels, *,
+                                                            precision="fp64", w_tilde_planes=None):
+    """numba.py:591-614 (the reference's public name keeps its 'wilde' spelling).
+
+    ``precision="mixed"`` runs the mixed likelihood's own double-float gathers
+    on w_tilde's (hi, lo) planes (``w_tilde_planes`` (2, M, M) float32, split
+    from ``w_tilde`` when not given) and returns F joined to float64.
+    """
     c = Call("curvature_matrix_via_w_wilde_sparse_mapping_matrix_from")
     W = c.arr(w_tilde, f64, 2, "w_tilde")
     idx, w = _sparse_inputs(c, pix_indexes_for_sub_slim_index, pix_weights_for_sub_slim_index)
     M, B, S = W.shape[0], idx.shape[1], int(pixels)
     out = c.empty((S, S))
+    if precision_code(precision) == _lib.AJ_MIXED:
+        if w_tilde_planes is None:
+            pl = c.empty((2, M, M), torch.float32)
+            _lib_call("aj_split_f64", ptr(W), M * M, ptr(pl[0]), ptr(pl[1]), c.stream())
+        else:
+            pl = c.arr(w_tilde_planes, torch.float32, 3, "w_tilde_planes")
+        ws = c.workspace(_lib.load().aj_curvature_w_tilde_sparse_mixed_workspace_size(M, B, S))
+        info = c.info()
+        _lib_call("aj_curvature_w_tilde_sparse_mixed", ptr(pl[0]), ptr(pl[1]), M, ptr(idx), ptr(w), B, S, ptr(out),
+                  ptr(ws), ws.numel(), ptr(info), c.stream())
+        c.check_info(info)
+        return c.out(out)
     ws = c.workspace(_lib.load().aj_sparse_workspace_size(M, B, S, M))
     info = c.info()
     _lib_call("aj_curvature_w_tilde_sparse", ptr(W), M, ptr(idx), ptr(w), B, S, ptr(out), ptr(ws), ws.numel(),
@@ -431,12 +449,15 @@ def log_likelihood_function_via_w_compact_from(dirty_image, data, noise_map, w_c
 
 def log_evidence_and_grad(dirty_image, data, noise_map, w_tilde, pix_indexes_for_sub_slim_index,
                           pix_weights_for_sub_slim_index, neighbors, neighbors_sizes, *, coefficient=1.0,
-                          precision="fp64", w_compact=None, native_index_for_slim_index=None):
+                          precision="fp64", w_compact=None, native_index_for_slim_index=None,
+                          return_reconstruction=False):
     """logE with its adjoint (no reference counterpart).
 
     Returns ``(logE, dlogE/dlambda, dlogE/dpix_weights)`` with lambda =
     coefficient**2; pass ``w_tilde=None`` with ``w_compact`` and
-    ``native_index_for_slim_index`` for the compact form.
+    ``native_index_for_slim_index`` for the compact form.  With
+    ``return_reconstruction=True`` the evaluation's own s = (F + H)^-1 D
+    (numba.py:699-731) comes fourth.
     """
     c = Call("log_evidence_and_grad")
     if w_tilde is not None:
@@ -446,11 +467,12 @@ def log_evidence_and_grad(dirty_image, data, noise_map, w_tilde, pix_indexes_for
         p = _problem(c, dirty_image, data, noise_map, pix_indexes_for_sub_slim_index, pix_weights_for_sub_slim_index,
                      neighbors, neighbors_sizes, coefficient, w_compact=w_compact,
                      native_index=native_index_for_slim_index)
-    out, gw, _ = _evidence(c, p, precision, True)
+    out, gw, rec = _evidence(c, p, precision, True)
     if c.numpy_out:
         o = out.cpu().numpy()
-        return float(o[0]), float(o[1]), gw.cpu().numpy()
-    return out[0], out[1], gw
+        res = (float(o[0]), float(o[1]), gw.cpu().numpy())
+        return res + (rec.cpu().numpy(),) if return_reconstruction else res
+    return (out[0], out[1], gw, rec) if return_reconstruction else (out[0], out[1], gw)
 
 
 LOG_TWO_PI = math.log(2.0 * math.pi)

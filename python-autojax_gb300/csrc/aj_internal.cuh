@@ -7,6 +7,10 @@ namespace aj {
 
 // ---- linalg.cu
 
+// columns per step of the float64 blocked Cholesky (linalg.cu); the no-allocation solve sizes its
+// fixed scratch with it
+constexpr int kSpdNB = 32;
+
 // C (m x n) = alpha op(A) op(B) + beta C, row-major float64.
 // lower_only: only tiles on or below the diagonal of C are touched (square C).
 int gemm_f64(bool transA, bool transB, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
@@ -60,6 +64,8 @@ struct Lanes {
 };
 // the lanes that forks from `caller` use on the current device (created on first use)
 int lanes_for(cudaStream_t caller, Lanes** out);
+// destroys the lanes of `caller` on the current device, if it has any
+int lanes_release(cudaStream_t caller);
 // lanes 0..n-1 start after the work already on st
 int lanes_fork(Lanes& l, cudaStream_t st, int n);
 // st continues after the work on lanes 0..n-1

@@ -65,6 +65,34 @@ using namespace aj;
 
 extern "C" {
 
+int aj_release_stream(void* stream) {
+    cudaStream_t st = as_stream(stream);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return AJ_ERR_CUDA;
+    Branches* br = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_branch_mu);
+        auto it = g_branches.find({dev, st});
+        if (it != g_branches.end()) {
+            br = it->second;
+            g_branches.erase(it);
+        }
+    }
+    int rc = AJ_OK;
+    if (br) {
+        for (int b = 0; b < kBranches; ++b) {
+            // each branch stream carries lanes of its own
+            if (lanes_release(br->s[b]) != AJ_OK) rc = AJ_ERR_CUDA;
+            if (cudaStreamDestroy(br->s[b]) != cudaSuccess || cudaEventDestroy(br->join[b]) != cudaSuccess)
+                rc = AJ_ERR_CUDA;
+        }
+        if (cudaEventDestroy(br->fork) != cudaSuccess) rc = AJ_ERR_CUDA;
+        delete br;
+    }
+    if (lanes_release(st) != AJ_OK) rc = AJ_ERR_CUDA;
+    return rc;
+}
+
 int aj_log_evidence_batched(const aj_problem* problems, int64_t n, int precision, int with_grad, double* out,
                             double* const* grad_weights, double* const* reconstruction, void* const* workspaces,
                             const size_t* workspace_bytes, int* info, void* stream) {

@@ -12,8 +12,12 @@
 // and stream capture records the same dependencies as graph edges.
 //
 // Streams and events are created once per (device, caller stream) on first
-// use and live until the process exits.  Keying by the caller's stream keeps
-// concurrent callers apart: evaluations enqueued on different streams (or
+// use and live until aj_release_stream(caller) or process exit (a caller that
+// makes a fresh stream per call should release each one when its work is
+// done; a later stream that happens to get the same handle value reuses the
+// set, which is harmless once the first stream's work has finished).
+// Keying by the caller's stream keeps concurrent callers apart: evaluations
+// enqueued on different streams (or
 // captured as parallel branches of one graph) each fork onto lanes of their
 // own, so their chains stay concurrent and never share an event.
 
@@ -63,6 +67,24 @@ int lanes_for(cudaStream_t caller, Lanes** out) {
     }
     *out = it->second;
     return AJ_OK;
+}
+
+int lanes_release(cudaStream_t caller) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return AJ_ERR_CUDA;
+    Lanes* l = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_lanes_mu);
+        auto it = g_lanes.find({dev, caller});
+        if (it == g_lanes.end()) return AJ_OK;
+        l = it->second;
+        g_lanes.erase(it);
+    }
+    bool ok = true;
+    for (int i = 0; i < kLaneCount; ++i) ok &= cudaStreamDestroy(l->s[i]) == cudaSuccess;
+    for (int i = 0; i < kLaneEvents; ++i) ok &= cudaEventDestroy(l->ev[i]) == cudaSuccess;
+    delete l;
+    return ok ? AJ_OK : AJ_ERR_CUDA;
 }
 
 int lanes_fork(Lanes& l, cudaStream_t st, int n) {

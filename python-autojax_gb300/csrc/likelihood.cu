@@ -450,6 +450,11 @@ size_t evidence_carve(const aj_problem* p, bool mixed, bool with_grad, void* bas
             b.TW = cv.take<double>(S * M);
             b.TWh = cv.take<float>(S * M);
             b.TWl = cv.take<float>(S * M);
+        } else if (M % 4 != 0) {
+            // the transposed Omega gather stores 4 columns (16 bytes) a row: other M gather T^T W
+            // row-major, then transpose
+            b.TWh = cv.take<float>(S * M);
+            b.TWl = cv.take<float>(S * M);
         }
         b.Omh = cv.take<float>(M * S);
         b.Oml = cv.take<float>(M * S);
@@ -631,10 +636,14 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
                 Wh = b.Wh;
                 Wl = b.Wl;
             }
-            // Omega = (T^T W)^T straight from the gather
-            AJ_TRY(csc_spmm_t_df_tr(b.cs, S, Wh, Wl, M, M, b.Omh, b.Oml, S, st));
+            if (M % 4 == 0) {
+                // Omega = (T^T W)^T straight from the gather (the planes must be 16-byte aligned)
+                AJ_TRY(csc_spmm_t_df_tr(b.cs, S, Wh, Wl, M, M, b.Omh, b.Oml, S, st));
+            } else {
+                AJ_TRY(csc_spmm_t_df(b.cs, S, Wh, Wl, M, M, b.TWh, b.TWl, M, st));
+            }
         }
-        if (b.compact) {
+        if (b.compact || M % 4 != 0) {
             AJ_TRY(transpose<float>(b.TWh, S, M, b.Omh, st));
             AJ_TRY(transpose<float>(b.TWl, S, M, b.Oml, st));
         }
@@ -714,6 +723,57 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         AJ_LAUNCHED();
     }
     return join_pre();
+}
+
+size_t aj_curvature_w_tilde_sparse_mixed_workspace_size(int64_t M, int64_t B, int64_t S) {
+    if (M < 0 || B < 0 || S <= 0) return 0;
+    Sizer z;
+    z.take<char>(csc_bytes(M, B, S));
+    z.take<float>(M * S);
+    z.take<float>(M * S);
+    z.take<float>(M * S);
+    z.take<float>(M * S);
+    z.take<float>(S * S);
+    z.take<float>(S * S);
+    return z.total();
+}
+
+int aj_curvature_w_tilde_sparse_mixed(const float* w_tilde_hi, const float* w_tilde_lo, int64_t M,
+                                      const int64_t* pix_indexes, const double* pix_weights, int64_t B, int64_t S,
+                                      double* out, void* workspace, size_t workspace_bytes, int* info, void* stream) {
+    if (M < 0 || B < 0 || S <= 0 || !out) return AJ_ERR_ARG;
+    if (M > 0 && (!w_tilde_hi || !w_tilde_lo || (B > 0 && (!pix_indexes || !pix_weights)))) return AJ_ERR_ARG;
+    if (!workspace || workspace_bytes < aj_curvature_w_tilde_sparse_mixed_workspace_size(M, B, S))
+        return AJ_ERR_WORKSPACE;
+    cudaStream_t st = as_stream(stream);
+    if (M == 0 || B == 0) return cudaMemsetAsync(out, 0, sizeof(double) * S * S, st) == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+    Carver cv(workspace, workspace_bytes);
+    Csc c;
+    {
+        char* at = cv.take<char>(csc_bytes(M, B, S));
+        Carver sub(at, csc_bytes(M, B, S));
+        csc_take(sub, M, B, S, c);
+    }
+    float* TWh = cv.take<float>(M * S);
+    float* TWl = cv.take<float>(M * S);
+    float* Omh = cv.take<float>(M * S);
+    float* Oml = cv.take<float>(M * S);
+    float* Fh = cv.take<float>(S * S);
+    float* Fl = cv.take<float>(S * S);
+    AJ_TRY(csc_build(pix_indexes, pix_weights, nullptr, M, B, S, CSC_SUM, c, info, st));
+    // the likelihood's own two gathers: Omega = (T^T W)^T, then F's lower triangle = T^T Omega
+    const bool tr = M % 4 == 0 && reinterpret_cast<uintptr_t>(w_tilde_hi) % 16 == 0 &&
+                    reinterpret_cast<uintptr_t>(w_tilde_lo) % 16 == 0;
+    if (tr) {
+        AJ_TRY(csc_spmm_t_df_tr(c, S, w_tilde_hi, w_tilde_lo, M, M, Omh, Oml, S, st));
+    } else {
+        AJ_TRY(csc_spmm_t_df(c, S, w_tilde_hi, w_tilde_lo, M, M, TWh, TWl, M, st));
+        AJ_TRY(transpose<float>(TWh, S, M, Omh, st));
+        AJ_TRY(transpose<float>(TWl, S, M, Oml, st));
+    }
+    AJ_TRY(csc_spmm_t_df(c, S, Omh, Oml, S, S, Fh, Fl, S, st, true));
+    AJ_TRY(df_mirror_lower(Fh, Fl, S, st));
+    return df_join(Fh, Fl, S * S, out, st);
 }
 
 }  // extern "C"

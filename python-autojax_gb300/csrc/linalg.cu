@@ -20,7 +20,7 @@
 
 namespace aj {
 
-constexpr int NB = 32;
+constexpr int NB = kSpdNB;
 
 __device__ __forceinline__ void lower_tile64(int64_t t, int64_t& bi, int64_t& bj) {
     int64_t r = static_cast<int64_t>((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);

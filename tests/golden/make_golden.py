@@ -386,4 +386,6 @@ def main(ref_root: str):
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    main(args[0] if args else "/root/reference")
+    if len(args) != 1:
+        sys.exit("usage: make_golden.py <path of the ickc/python-autojax checkout>")
+    main(args[0])

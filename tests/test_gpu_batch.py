@@ -201,3 +201,26 @@ def _crowded_setup():
     d = synthetic.make_dataset("cfg1", K=600, seed=6)
     W = aj.w_tilde_curvature_interferometer_from(d["noise_map_real"], d["uv_wavelengths"], d["grid_radians_slim"])
     return d, W
+
+
+def test_release_stream_frees_and_recreates_side_streams(setup):
+    """aj_release_stream drops the lanes and branches of a caller stream; the next call on the
+    stream builds a fresh set and gives bit-identical results."""
+    import torch
+
+    from autojax_gb300 import _lib
+
+    lib = _lib.load()
+    batch = _batch(setup, "mixed")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        batch.launch()
+    s.synchronize()
+    first = batch.out.cpu().numpy().copy()
+    assert lib.aj_release_stream(s.cuda_stream) == _lib.AJ_OK
+    assert lib.aj_release_stream(s.cuda_stream) == _lib.AJ_OK  # nothing left to free
+    with torch.cuda.stream(s):
+        batch.launch()
+    s.synchronize()
+    np.testing.assert_array_equal(batch.out.cpu().numpy(), first)
+    assert lib.aj_release_stream(s.cuda_stream) == _lib.AJ_OK

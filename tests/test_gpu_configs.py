@@ -1,0 +1,195 @@
+"""Parity at the benchmark sizes, against the oracle on the same inputs.
+
+Two configurations: K = 1e5 visibilities with M = 5,024 image pixels and S = 1,000
+Delaunay source pixels (80 x 80 at 0.05", r = 2"), and K = 1e6 with M = 9,504 and
+S = 1,500 (100 x 100 at 0.04", r = 2.4").  Every size exercises the multi-chunk
+gathers (M > 1,024) and the multi-panel factorisations (S > 1,024 at K = 1e6).
+
+* w_tilde (numba.py:156-207): the GPU's float64 W~ (compact table + expansion at
+  full K) on sampled entries against the oracle's sum over every visibility; the
+  direct builds (float64 and mixed) on a visibility sample against each other and
+  against the oracle.
+* F (numba.py:410-435), D (numba.py:380-406), s (numba.py:699-731) and logE
+  (numba.py:761-857) with its adjoint: both sides take the GPU's float64 W~ (the
+  oracle's own M x M sum over 1e6 visibilities would take hours on the host).
+
+Tolerances: float64 path rel 1e-10 (entries that cancel judged against 1e-11 of
+the result's scale); s against cond(A) as in the golden solve test; the mixed
+path as each test states.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import adjoint
+from oracle import numpy_port as ref
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+ATOL_FRAC = 1e-11
+LAMBDAS = (1e-3, 1e3)
+
+
+@pytest.fixture(scope="module", params=["cfg2", "cfg3"])
+def cfg(request):
+    import torch
+
+    import autojax_gb300 as aj
+    from autojax_gb300 import synthetic
+
+    d = synthetic.make_dataset(request.param)
+    dev = torch.device("cuda", 0)
+    n = torch.from_numpy(d["noise_map_real"]).to(dev)
+    uv = torch.from_numpy(d["uv_wavelengths"]).to(dev)
+    wc = aj.w_compact_curvature_interferometer_from(d["grid_size"], n, uv, d["pixel_scale"])
+    Wd = aj.w_tilde_via_compact_from(wc, torch.from_numpy(d["native_index_for_slim_index"]).to(dev))
+    W = Wd.cpu().numpy()
+    T = ref.mapping_matrix_from(d["pix_indexes_for_sub_slim_index"], d["pix_weights_for_sub_slim_index"], d["S"])
+    yield {"d": d, "W": W, "Wd": Wd, "T": T}
+    del Wd
+    torch.cuda.empty_cache()
+
+
+def _args(d, W):
+    return (d["dirty_image"], d["data"], d["noise_map"], W, d["pix_indexes_for_sub_slim_index"],
+            d["pix_weights_for_sub_slim_index"], d["neighbors"], d["neighbors_sizes"])
+
+
+def _entries(M, seed=0):
+    rng = np.random.default_rng(seed)
+    rows = np.repeat(np.array([0, M // 3, M // 2, M - 1]), 48)
+    cols = rng.integers(0, M, rows.size)
+    cols[::48] = rows[::48]  # the diagonal too
+    return rows, cols
+
+
+def test_w_tilde_full_k_entries_match_oracle(cfg):
+    d, W = cfg["d"], cfg["W"]
+    rows, cols = _entries(d["M"])
+    exp = ref.w_tilde_entries(d["noise_map_real"], d["uv_wavelengths"], d["grid_radians_slim"], rows, cols)
+    scale = float(np.abs(np.diag(W)).max())
+    np.testing.assert_allclose(W[rows, cols], exp, rtol=RTOL, atol=ATOL_FRAC * scale)
+    assert np.array_equal(W, W.T)
+
+
+def test_direct_w_tilde_builds_match_oracle(cfg):
+    """The direct builds at the configuration's M on a 4,096-visibility sample."""
+    import autojax_gb300 as aj
+
+    d = cfg["d"]
+    Ks = 4096
+    n, uv, g = d["noise_map_real"][:Ks].copy(), d["uv_wavelengths"][:Ks].copy(), d["grid_radians_slim"]
+    W64 = aj.w_tilde_curvature_interferometer_from(n, uv, g)
+    Wmx, P = aj.w_tilde_curvature_interferometer_from(n, uv, g, precision="mixed", planes=True)
+    rows, cols = _entries(d["M"], seed=1)
+    exp = ref.w_tilde_entries(n, uv, g, rows, cols)
+    scale = float(np.abs(np.diag(W64)).max())
+    np.testing.assert_allclose(W64[rows, cols], exp, rtol=RTOL, atol=ATOL_FRAC * scale)
+    # mixed: ~1e-12 of the scale (float64 panel, exact digit products or double-float sums)
+    np.testing.assert_allclose(Wmx, W64, rtol=0, atol=1e-12 * scale)
+    np.testing.assert_allclose(Wmx[rows, cols], exp, rtol=0, atol=1e-12 * scale)
+    np.testing.assert_allclose(P[0].astype(np.float64) + P[1].astype(np.float64), Wmx, rtol=0, atol=1e-15 * scale)
+
+
+def test_fp64_products_match_oracle(cfg):
+    import torch
+
+    import autojax_gb300 as aj
+
+    d, W, T = cfg["d"], cfg["W"], cfg["T"]
+    dev = cfg["Wd"].device
+    idx = torch.from_numpy(d["pix_indexes_for_sub_slim_index"]).to(dev)
+    w = torch.from_numpy(d["pix_weights_for_sub_slim_index"]).to(dev)
+    F = aj.curvature_matrix_via_w_wilde_sparse_mapping_matrix_from(cfg["Wd"], idx, w, d["S"]).cpu().numpy()
+    F_ref = ref.curvature_matrix_via_w_tilde_from(W, T)
+    np.testing.assert_allclose(F, F_ref, rtol=RTOL, atol=ATOL_FRAC * np.abs(F_ref).max())
+    D = aj.data_vector_from(T, d["dirty_image"])
+    D_ref = ref.data_vector_from(T, d["dirty_image"])
+    np.testing.assert_allclose(D, D_ref, rtol=RTOL, atol=ATOL_FRAC * np.abs(D_ref).max())
+    Tg = aj.mapping_matrix_from(d["pix_indexes_for_sub_slim_index"], d["pix_weights_for_sub_slim_index"], d["S"])
+    np.testing.assert_array_equal(Tg, T)
+
+
+@pytest.mark.parametrize("lam", LAMBDAS)
+def test_fp64_solve_matches_oracle(cfg, lam):
+    import autojax_gb300 as aj
+
+    d, W, T = cfg["d"], cfg["W"], cfg["T"]
+    H = ref.constant_regularization_matrix_from(np.sqrt(lam), d["neighbors"], d["neighbors_sizes"])
+    A = ref.curvature_matrix_via_w_tilde_from(W, T) + H
+    D = ref.data_vector_from(T, d["dirty_image"])
+    s = aj.reconstruction_positive_negative_from(D, A)
+    exp = ref.reconstruction_positive_negative_from(D, A)
+    ev = np.linalg.eigvalsh(A)
+    cond = ev[-1] / ev[0]
+    err = np.linalg.norm(s - exp) / np.linalg.norm(exp)
+    assert err <= max(1e-13, 1e-15 * cond), (err, cond)
+    res = np.linalg.norm(A @ s - D) / (np.linalg.norm(A) * np.linalg.norm(s))
+    assert res < 1e-13, res
+
+
+@pytest.mark.parametrize("lam", LAMBDAS)
+def test_fp64_log_evidence_matches_oracle(cfg, lam):
+    import autojax_gb300 as aj
+
+    d = cfg["d"]
+    c = float(np.sqrt(lam))
+    logE, dlam, gw, s = aj.log_evidence_and_grad(*_args(d, cfg["Wd"]), coefficient=c, precision="fp64",
+                                                  return_reconstruction=True)
+    logE, dlam, gw, s = float(logE), float(dlam), gw.cpu().numpy(), s.cpu().numpy()
+    a = _args(d, cfg["W"])
+    r_logE, r_dlam, r_gw = adjoint.log_evidence_and_grad(*a, coefficient=c)
+    assert abs(logE - r_logE) <= RTOL * abs(r_logE), (logE, r_logE)
+    plain = ref.log_likelihood_function_via_w_tilde_from(*a, coefficient=c)
+    assert abs(logE - plain) <= RTOL * abs(plain), (logE, plain)
+    # s, dlogE/dlambda and the weight gradient go through A^-1: judged against cond(A)
+    H = ref.constant_regularization_matrix_from(c, d["neighbors"], d["neighbors_sizes"])
+    A = ref.curvature_matrix_via_w_tilde_from(cfg["W"], cfg["T"]) + H
+    D = ref.data_vector_from(cfg["T"], d["dirty_image"])
+    ev = np.linalg.eigvalsh(A)
+    cond = ev[-1] / ev[0]
+    s_ref = np.linalg.solve(A, D)
+    assert np.linalg.norm(s - s_ref) / np.linalg.norm(s_ref) <= max(1e-13, 1e-15 * cond)
+    trace_scale = d["S"] / lam
+    assert abs(dlam - r_dlam) <= max(1e-10, 1e-15 * cond) * trace_scale + 1e-8 * abs(r_dlam), (dlam, r_dlam)
+    np.testing.assert_allclose(gw, r_gw, rtol=0, atol=max(1e-9, 1e-15 * cond) * np.abs(r_gw).max())
+
+
+@pytest.mark.parametrize("lam", LAMBDAS)
+def test_mixed_matches_oracle(cfg, lam):
+    """The mixed path against the float64 oracle on the same W~.
+
+    Stated tolerances: logE rel 1e-7 (the target is 1e-6); F 1e-12 of its scale
+    (double-float gathers, ~2^-47 a term); s against cond(A) at double-float
+    rounding (2^-47 cond); dlogE/dlambda and the weight gradient as in the
+    small-case mixed tests.
+    """
+    import torch
+
+    import autojax_gb300 as aj
+
+    d, W, T = cfg["d"], cfg["W"], cfg["T"]
+    c = float(np.sqrt(lam))
+    logE, dlam, gw, s = aj.log_evidence_and_grad(*_args(d, cfg["Wd"]), coefficient=c, precision="mixed",
+                                                  return_reconstruction=True)
+    logE, dlam, gw, s = float(logE), float(dlam), gw.cpu().numpy(), s.cpu().numpy()
+    r_logE, r_dlam, r_gw = adjoint.log_evidence_and_grad(*_args(d, W), coefficient=c)
+    assert abs(logE - r_logE) <= 1e-7 * abs(r_logE), (logE, r_logE, abs(logE - r_logE) / abs(r_logE))
+    dev = cfg["Wd"].device
+    F = aj.curvature_matrix_via_w_wilde_sparse_mapping_matrix_from(
+        cfg["Wd"], torch.from_numpy(d["pix_indexes_for_sub_slim_index"]).to(dev),
+        torch.from_numpy(d["pix_weights_for_sub_slim_index"]).to(dev), d["S"], precision="mixed").cpu().numpy()
+    F_ref = ref.curvature_matrix_via_w_tilde_from(W, T)
+    np.testing.assert_allclose(F, F_ref, rtol=0, atol=1e-12 * np.abs(F_ref).max())
+    H = ref.constant_regularization_matrix_from(c, d["neighbors"], d["neighbors_sizes"])
+    A = F_ref + H
+    ev = np.linalg.eigvalsh(A)
+    cond = ev[-1] / ev[0]
+    s_ref = np.linalg.solve(A, ref.data_vector_from(T, d["dirty_image"]))
+    assert np.linalg.norm(s - s_ref) / np.linalg.norm(s_ref) <= max(1e-10, 2.0**-47 * cond)
+    trace_scale = d["S"] / lam
+    assert abs(dlam - r_dlam) <= 1e-6 * trace_scale + 1e-5 * abs(r_dlam), (dlam, r_dlam)
+    np.testing.assert_allclose(gw, r_gw, rtol=0, atol=max(1e-5, 2e-15 * cond) * np.abs(r_gw).max())

@@ -95,3 +95,18 @@ def test_adjoint_gradients_match_finite_differences(case, coef):
         fd = (f(wp, lam) - f(wm, lam)) / (2 * hw)
         scale = max(1.0, float(np.max(np.abs(gw))))
         assert abs(fd - gw[m, b]) <= 2e-5 * scale, (m, b, fd, gw[m, b])
+
+
+@pytest.mark.parametrize("case", ["refgen", "cfg1"])
+def test_w_tilde_entries_and_separable_table_match_the_pinned_oracle(case):
+    """The two host helpers the large-size checks use (sampled W~ entries, and the offset
+    table by a separable complex product) against the golden-pinned oracle sums."""
+    d = gu.full_inputs(case)
+    W = d["w_tilde"]
+    M = W.shape[0]
+    rng = np.random.default_rng(4)
+    rows, cols = rng.integers(0, M, 300), rng.integers(0, M, 300)
+    e = ref.w_tilde_entries(d["noise_map_real"], d["uv_wavelengths"], d["grid_radians_slim"], rows, cols)
+    np.testing.assert_allclose(e, W[rows, cols], rtol=1e-12, atol=1e-13 * np.abs(W).max())
+    wc = ref.w_compact_separable(d["grid_size"], d["noise_map_real"], d["uv_wavelengths"], d["pixel_scale"])
+    np.testing.assert_allclose(wc, d["w_compact"], rtol=1e-11, atol=1e-12 * np.abs(d["w_compact"]).max())

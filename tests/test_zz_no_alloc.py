@@ -45,8 +45,9 @@ def test_noalloc_solve_matches_workspace_solve_twice():
 
     lib = _lib.load()
     st = torch.cuda.current_stream().cuda_stream
-    # two calls in a row, different sizes: the shared scratch keeps the first call's contents
-    for S, seed in ((1000, 1), (257, 2)):
+    # calls in a row, different sizes (the capacity itself first): the shared scratch keeps the
+    # previous call's contents
+    for S, seed in ((_lib.AJ_NOALLOC_SOLVE_MAX_S, 3), (1000, 1), (257, 2)):
         A_np, b_np = _spd(S, seed)
         A = torch.from_numpy(A_np).cuda()
         b = torch.from_numpy(b_np).cuda()
@@ -69,3 +70,19 @@ def test_noalloc_solve_rejects_sizes_above_capacity():
     S = _lib.AJ_NOALLOC_SOLVE_MAX_S + 1
     rc = lib.aj_spd_solve_noalloc(None, None, S, None, None, torch.cuda.current_stream().cuda_stream)
     assert rc == _lib.AJ_ERR_TOO_LARGE
+
+
+def test_noalloc_solve_requires_info():
+    """A non-positive-definite A is reported only through info, so a NULL info is rejected."""
+    import torch
+
+    from autojax_gb300 import _lib
+
+    lib = _lib.load()
+    S = 8
+    A = torch.eye(S, dtype=torch.float64, device="cuda")
+    b = torch.ones(S, dtype=torch.float64, device="cuda")
+    out = torch.empty(S, dtype=torch.float64, device="cuda")
+    rc = lib.aj_spd_solve_noalloc(b.data_ptr(), A.data_ptr(), S, out.data_ptr(), None,
+                                  torch.cuda.current_stream().cuda_stream)
+    assert rc == _lib.AJ_ERR_ARG
