@@ -82,12 +82,24 @@ int aj_slim_from_mask(const uint8_t* mask, int64_t ny, int64_t nx, const double*
  * sqrt(w)-scaled cos/sin panels (exact identity cos(a-b) = cos a cos b +
  * sin a sin b). out64 (M, M) is always written; out_planes (2, M, M), may
  * be NULL, receives the double-float planes (hi then lo) the mixed
- * likelihood reads. AJ_MIXED evaluates the panel in float64 and the product
- * in double-float on the float32 pipe. */
+ * likelihood reads. AJ_MIXED evaluates the panel in float64, cuts each value
+ * into 7 exact 7-bit integer digits (48 bits) and sums the digit products on
+ * the bf16 tensor cores (tcgen05, float32 accumulators holding exact integers),
+ * folded into double-float; a bounded wait that expires (a fault of the
+ * device, not of the data) leaves NaN in out64[0]. */
 size_t aj_w_tilde_curvature_workspace_size(int64_t K, int64_t M, int precision);
 int aj_w_tilde_curvature(const double* noise_map_real, const double* uv, const double* grid_slim, int64_t K,
                          int64_t M, double* out64, float* out_planes, void* workspace, size_t workspace_bytes,
                          int precision, void* stream);
+
+/* Test probe of the tensor-core digit product behind AJ_MIXED w_tilde (no
+ * reference counterpart). digits: [7][Mp][rows] bf16 integers (|d| <= 64),
+ * Mp = M rounded up to 128, rows a multiple of 256. For i >= j < M writes
+ * out (+)= scale * sum_{d+e<=6} 2^(-7(d+e)) sum_r digits[d][i][r] digits[e][j][r]
+ * as double-float planes out_hi/out_lo (M, M); `scale` and `err` are device
+ * words (err != 0 after a wait expired). */
+int aj_digit_syrk_probe(const void* digits, int64_t rows, int64_t M, float* out_hi, float* out_lo,
+                        const float* scale, int accumulate, int* err, void* stream);
 
 /* numba.py:211-234 w_compact_curvature_interferometer_from.
  * out (N, 2N-1): w_c[n0][n1+N-1] = sum_k noise_k^-2 cos(D (n1 u_k - n0 v_k)),

@@ -68,6 +68,7 @@ SIGNATURES = {
     "aj_slim_from_mask": (INT, [P, I64, I64, P, I64, P, P, P, P]),
     "aj_w_tilde_curvature_workspace_size": (SZ, [I64, I64, INT]),
     "aj_w_tilde_curvature": (INT, [P, P, P, I64, I64, P, P, P, SZ, INT, P]),
+    "aj_digit_syrk_probe": (INT, [P, I64, I64, P, P, P, INT, P, P]),
     "aj_w_compact_curvature_workspace_size": (SZ, [I64, I64, INT]),
     "aj_w_compact_curvature": (INT, [I64, P, P, I64, D, P, P, SZ, INT, P]),
     "aj_w_tilde_preload_workspace_size": (SZ, [I64, I64, I64, INT]),

@@ -113,6 +113,13 @@ int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, c
                         float* xh = nullptr, float* xl = nullptr);
 int df_frob_lower(const float* h, const float* l, int64_t S, double* partial, int64_t nparts, cudaStream_t st);
 
+// ---- wtilde_tc.cu (the mixed direct w_tilde on the tensor cores)
+
+size_t wtilde_tc_workspace_bytes(int64_t K, int64_t M);
+// ph/pl (M x M) receive the lower triangle of W = sum_k w_k cos(...) as double-float planes
+int wtilde_tc(const double* sigma, const double* uv, const double* grid, int64_t K, int64_t M, float* ph, float* pl,
+              void* ws, size_t bytes, cudaStream_t st);
+
 // ---- mapping.cu
 
 // H = 1e-8 I + c^2 L (numba.py:686-694); c read from coefficient_dev when it is not null

@@ -132,31 +132,6 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// Double-float panel: float64 sincospi of the phase, scaled by sqrt(w), split into hi/lo planes.
-__global__ void wtilde_panel_df_kernel(const double* __restrict__ sigma, const double* __restrict__ uv,
-                                       const double* __restrict__ grid, int64_t K, int64_t M, int64_t k0, int64_t kc,
-                                       int64_t Mp, float* __restrict__ Ph, float* __restrict__ Pl) {
-    const int64_t kk = blockIdx.x;
-    const int64_t i = blockIdx.y * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= Mp) return;
-    const int64_t k = k0 + kk;
-    double c = 0.0, s = 0.0;
-    if (k < K && i < M) {
-        const double u = uv[2 * k], v = uv[2 * k + 1];
-        const double t = fma(grid[2 * i + 1], u, grid[2 * i] * v);
-        const double sw = 1.0 / fabs(sigma[k]);
-        double sd, cd;
-        sincospi(2.0 * t, &sd, &cd);
-        c = cd * sw;
-        s = sd * sw;
-    }
-    const float ch = __double2float_rn(c), sh = __double2float_rn(s);
-    Ph[kk * Mp + i] = ch;
-    Pl[kk * Mp + i] = __double2float_rn(c - (double)ch);
-    Ph[(kc + kk) * Mp + i] = sh;
-    Pl[(kc + kk) * Mp + i] = __double2float_rn(s - (double)sh);
-}
-
 // --------------------------------------------------------------- compact
 
 // Tab[q][kk][n] for q = 0..3: sqrt(w) {cos, sin}(2 pi ps n u_k), {cos, sin}(2 pi ps n v_k), n < N.
@@ -530,12 +505,15 @@ using namespace aj;
 extern "C" {
 
 size_t aj_w_tilde_curvature_workspace_size(int64_t K, int64_t M, int precision) {
+    if (precision == AJ_MIXED) {
+        // the digit panel; the planes may also be joined through this buffer
+        size_t b = wtilde_tc_workspace_bytes(K, M);
+        if (b < sizeof(double) * M * M) b = sizeof(double) * M * M;
+        return align_up(b);
+    }
     WtildePlan p = wtilde_plan(K, M);
-    size_t panel = 2 * p.kc * p.Mp * p.elem;
-    // the mixed path may join its double-float planes through this buffer
-    if (precision == AJ_MIXED && panel < sizeof(double) * M * M) panel = sizeof(double) * M * M;
     Sizer s;
-    s.take<char>(panel);
+    s.take<char>(2 * p.kc * p.Mp * p.elem);
     return s.total();
 }
 
@@ -563,17 +541,8 @@ int aj_w_tilde_curvature(const double* noise_map_real, const double* uv, const d
             ph = reinterpret_cast<float*>(out64);
             pl = ph + M * M;  // out64 holds exactly 2 M^2 floats
         }
-        float* Ph = static_cast<float*>(workspace);
-        float* Pl = Ph + 2 * p.kc * p.Mp;
-        for (int64_t ch = 0; ch < p.nchunk; ++ch) {
-            const int64_t k0 = ch * p.kc;
-            dim3 pg((unsigned)p.kc, (unsigned)((p.Mp + 255) / 256));
-            wtilde_panel_df_kernel<<<pg, 256, 0, st>>>(noise_map_real, uv, grid_slim, K, M, k0, p.kc, p.Mp, Ph, Pl);
-            AJ_LAUNCHED();
-            // W (+)= P^T P on lower 64x64 tiles
-            AJ_TRY(gemm_df(true, false, M, M, 2 * p.kc, false, Ph, Pl, p.Mp, Ph, Pl, p.Mp, ch > 0, ph, pl, M, true,
-                           false, st));
-        }
+        // W's lower triangle from exact digit products on the tensor cores (wtilde_tc.cu)
+        AJ_TRY(wtilde_tc(noise_map_real, uv, grid_slim, K, M, ph, pl, workspace, workspace_bytes, st));
         AJ_TRY(df_mirror_lower(ph, pl, M, st));
         if (own) {
             // planes live in out64's storage: join in place from the back is unsafe, so join via the panel buffer

@@ -1,0 +1,599 @@
+// Mixed-precision direct w_tilde on the Blackwell tensor cores (numba.py:156-207).
+//
+// W = P^T P with P[r][i] = sqrt(w_k) {cos, sin}(2 pi t_ik) (the cos rows, then the
+// sin rows, of one chunk of visibilities).  The float64 panel values are cut into
+// exact integer digits and the product runs as a sum of exact digit products on
+// the bf16 tensor pipe (an Ozaki-style split):
+//
+//   y = P / s in [-1, 1] (s a power of two >= max sqrt(w_k)),
+//   y = sum_d delta_d 2^-(B0 + B d),  delta_d integers, |delta_d| <= 2^(B-1),
+//
+// with B = 7 bits a digit (B0 = 6 for the first), kDigits = 7 digits: 48 bits,
+// the residual below 2^-48 of s.  A digit is exact in bf16, and a product of two
+// is an integer of at most 2^12; the products of one "level" L = d + e share
+// the scale 2^-(2 B0 + B L), so for every level a tcgen05.mma (M = 128, N = 64,
+// K = 16) sums the digit products of its L + 1 pairs into one float32 TMEM
+// accumulator.  Over a group of kGroupRows rows a level sum stays below
+// (L + 1) kGroupRows 2^12 <= 7 * 256 * 4096 = 2^22.8, so every partial sum is an
+// integer the float32 accumulator holds exactly.  Levels above kDigits - 1 are
+// dropped: they are below 2^-48 of s^2 per term, the panel's own rounding.
+// After each group the epilogue warps read the level sums out of TMEM and fold
+// them, scaled by powers of two (exact), into double-float accumulators with
+// TwoSum (error-free but for the low word's rounding, ~2^-48 relative).
+//
+// Layout: the digit panel is [kDigits][Mp][Rc] bf16 (k fastest), loaded by TMA as
+// one 3-D box per operand and stage (all digits of a 32-row k slab, 64-byte
+// rows, 64-byte swizzle), the canonical K-major layout the shared-memory matrix
+// descriptors name.  One CTA computes one 128 x 64 tile of the lower block
+// triangle over the whole chunk: warp 0 issues the TMA loads, warp 1 (one
+// thread) the MMAs and owns the TMEM allocation, warps 2-5 run the epilogue.
+// Every wait on an mbarrier is bounded (seconds, by the global timer): on
+// expiry the CTA sets an error word, drains what it issued and frees its TMEM.
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <math.h>
+
+#include <mutex>
+
+#include "aj_internal.cuh"
+
+namespace aj {
+
+namespace tc {
+
+constexpr int kDigits = 7;
+constexpr int kDigitBits = 7;
+constexpr int kFirstBits = 6;  // y in [-1, 1]: the first digit rint(y 2^6) lies in [-64, 64]
+constexpr int kLevels = kDigits;            // levels 0 .. kDigits - 1
+constexpr int BM = 128, BN = 64, BK = 32;   // tile rows, tile columns, k rows a stage
+constexpr int kGroupRows = 256;             // rows summed in TMEM between epilogue folds
+constexpr int kStagesPerGroup = kGroupRows / BK;
+constexpr int kStageA = kDigits * BM * BK * 2;  // bytes
+constexpr int kStageB = kDigits * BN * BK * 2;
+constexpr int kStageBytes = kStageA + kStageB;
+constexpr int kStages = 2;
+constexpr int kTmemCols = 512;              // >= kLevels * BN, a power of two
+constexpr int kThreads = 192;
+constexpr size_t kSmemBytes = size_t(kStages) * kStageBytes + 1024 + 256;
+constexpr unsigned long long kWaitNs = 4ull * 1000 * 1000 * 1000;  // 4 s (a stage takes microseconds)
+
+static_assert(kLevels * BN <= kTmemCols, "level accumulators exceed TMEM");
+static_assert((kLevels) * kGroupRows * (1 << (2 * (kDigitBits - 1))) < (1 << 23), "level sums must stay exact");
+static_assert(kGroupRows % BK == 0, "group of whole stages");
+static_assert(kSmemBytes <= 232448, "shared memory");
+
+// error word bits
+constexpr int kErrTimeout = 1;
+
+struct Shared {
+    uint64_t full[kStages];
+    uint64_t empty[kStages];
+    uint64_t accfull;
+    uint64_t accempty;
+    uint64_t mmadone;
+    uint32_t tmem_base;
+    int abort;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the phase with the given parity to complete; false once the CTA is aborting or the
+// wait ran past its limit (which starts the abort).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort, int* err) {
+    unsigned long long t0 = 0;
+    for (uint32_t n = 0;; ++n) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((n & 255) == 255) {
+            // an expired wait anywhere in the grid ends every CTA's work
+            if (*abort || *reinterpret_cast<volatile int*>(err)) {
+                *abort = 1;
+                return false;
+            }
+            const unsigned long long t = global_ns();
+            if (t0 == 0) {
+                t0 = t;
+            } else if (t - t0 > kWaitNs) {
+                *abort = 1;
+                atomicOr(err, kErrTimeout);
+                return false;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// 32 consecutive float32 columns of this warp's 32 TMEM lanes (lane = thread)
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// K-major operand in shared memory, 64-byte rows with the 64-byte swizzle, 8-row groups 512 bytes apart.
+__device__ __forceinline__ uint64_t desc_sw64(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);  // start address
+    d |= static_cast<uint64_t>(1) << 16;                   // leading byte offset (unused by swizzled K-major)
+    d |= static_cast<uint64_t>(512 >> 4) << 32;            // stride byte offset: next 8-row group
+    d |= static_cast<uint64_t>(1) << 46;                   // descriptor version
+    d |= static_cast<uint64_t>(4) << 61;                   // 64-byte swizzle
+    return d;
+}
+
+// kind::f16 instruction descriptor: float32 accumulator, bf16 A and B, both K-major, M = 128, N = 64.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(BN >> 3) << 17) | (uint32_t(BM >> 4) << 24);
+
+// lower block-triangle tile t -> (row tile I of 128 rows, column tile J of 64 columns), J <= 2I + 1
+__device__ __forceinline__ void tile_of(int64_t t, int64_t& I, int64_t& J) {
+    // tiles before row I: I (I + 1)
+    int64_t r = static_cast<int64_t>((sqrt(4.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (r * (r + 1) > t) --r;
+    while ((r + 1) * (r + 2) <= t) ++r;
+    I = r;
+    J = t - r * (r + 1);
+}
+
+__device__ __forceinline__ void two_sum_into(float& hi, float& lo, float c) {
+    const float s = hi + c;
+    const float bb = s - hi;
+    const float e = (hi - (s - bb)) + (c - bb);
+    hi = s;
+    lo += e;
+}
+
+// Out (+)= s2 * acc on the lower triangle of one 128 x 64 tile, as double-float planes.
+__device__ __forceinline__ void store_row(float* __restrict__ oh, float* __restrict__ ol, int64_t ld, int64_t M,
+                                          int64_t gi, int64_t gj0, const float (&h)[BN], const float (&l)[BN],
+                                          float scale, int accumulate) {
+    if (gi >= M) return;
+#pragma unroll
+    for (int j = 0; j < BN; ++j) {
+        const int64_t gj = gj0 + j;
+        if (gj > gi || gj >= M) continue;
+        float ah = h[j] * scale, al = l[j] * scale;
+        if (accumulate) {
+            const float bh = oh[gi * ld + gj], bl = ol[gi * ld + gj];
+            const float s = ah + bh;
+            const float bb = s - ah;
+            float e = (ah - (s - bb)) + (bh - bb);
+            e += al + bl;
+            ah = s + e;
+            al = e - (ah - s);
+        } else {
+            const float s = ah + al;
+            al = al - (s - ah);
+            ah = s;
+        }
+        oh[gi * ld + gj] = ah;
+        ol[gi * ld + gj] = al;
+    }
+}
+
+// One CTA per lower tile; Rc rows of digits (a multiple of kGroupRows).  s2 = s^2 2^-(2 first bits).
+__global__ void __launch_bounds__(kThreads, 1)
+    digit_syrk_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                      int64_t Rc, int64_t M, float* __restrict__ out_h, float* __restrict__ out_l, int64_t ld,
+                      const float* __restrict__ scale_dev, int accumulate, int* __restrict__ err) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    Shared* sh = reinterpret_cast<Shared*>(base + size_t(kStages) * kStageBytes);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int64_t I, J;
+    tile_of(blockIdx.x, I, J);
+    const int ngroups = static_cast<int>(Rc / kGroupRows);
+    const int nstages = ngroups * kStagesPerGroup;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&sh->full[s], 1);
+            mbar_init(&sh->empty[s], 1);
+        }
+        mbar_init(&sh->accfull, 1);
+        mbar_init(&sh->accempty, 4);
+        mbar_init(&sh->mmadone, 1);
+        sh->abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem_base)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = sh->tmem_base;
+    volatile int* abort = &sh->abort;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // producer: every stage holds all digits of one 32-row slab of both operands
+            int issued = 0;
+            for (int it = 0; it < nstages; ++it) {
+                const int s = it % kStages;
+                if (it >= kStages && !mbar_wait(&sh->empty[s], ((it / kStages) & 1) ^ 1, abort, err)) break;
+                unsigned char* sa = base + size_t(s) * kStageBytes;
+                mbar_expect_tx(&sh->full[s], kStageBytes);
+                tma_load_3d(sa, &map_a, it * BK, static_cast<int>(I * BM), 0, &sh->full[s]);
+                tma_load_3d(sa + kStageA, &map_b, it * BK, static_cast<int>(J * BN), 0, &sh->full[s]);
+                ++issued;
+            }
+            // drain: every issued load lands before the CTA may leave (a no-op on the normal path,
+            // where the MMA thread consumed them all)
+            for (int it = (issued > kStages ? issued - kStages : 0); it < issued && *abort; ++it) {
+                const int s = it % kStages;
+                unsigned long long t0 = global_ns();
+                while (!mbar_try_wait(&sh->full[s], (it / kStages) & 1) && global_ns() - t0 < kWaitNs) {
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t sbase = smem_u32(base);
+            for (int g = 0; g < ngroups && !*abort; ++g) {
+                if (g > 0 && !mbar_wait(&sh->accempty, (g - 1) & 1, abort, err)) break;
+                tc_fence_after();
+                bool ok = true;
+                for (int sg = 0; sg < kStagesPerGroup; ++sg) {
+                    const int it = g * kStagesPerGroup + sg;
+                    const int s = it % kStages;
+                    if (!mbar_wait(&sh->full[s], (it / kStages) & 1, abort, err)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t sa = sbase + static_cast<uint32_t>(s * kStageBytes);
+                    const uint32_t sb = sa + kStageA;
+#pragma unroll
+                    for (int ks = 0; ks < BK / 16; ++ks) {
+#pragma unroll
+                        for (int L = 0; L < kLevels; ++L) {
+#pragma unroll
+                            for (int d = 0; d <= L; ++d) {
+                                const int e = L - d;
+                                const uint64_t ad = desc_sw64(sa + d * (BM * BK * 2) + ks * 32);
+                                const uint64_t bd = desc_sw64(sb + e * (BN * BK * 2) + ks * 32);
+                                const uint32_t acc = (sg == 0 && ks == 0 && d == 0) ? 0u : 1u;
+                                tc_mma(tmem + static_cast<uint32_t>(L * BN), ad, bd, kIdesc, acc);
+                            }
+                        }
+                    }
+                    tc_commit(&sh->empty[s]);
+                }
+                if (!ok) break;
+                tc_commit(&sh->accfull);
+            }
+            // every MMA this thread issued completes before the TMEM is freed
+            tc_commit(&sh->mmadone);
+            const unsigned long long t0 = global_ns();
+            while (!mbar_try_wait(&sh->mmadone, 0) && global_ns() - t0 < kWaitNs) {
+            }
+        }
+    } else {
+        // epilogue: warp w reads TMEM lanes 32 (w % 4) ..
+        const int q = warp & 3;
+        const uint32_t lane_addr = tmem + (static_cast<uint32_t>(q * 32) << 16);
+        float h[BN], l[BN];
+#pragma unroll
+        for (int j = 0; j < BN; ++j) {
+            h[j] = 0.f;
+            l[j] = 0.f;
+        }
+        for (int g = 0; g < ngroups; ++g) {
+            if (!mbar_wait(&sh->accfull, g & 1, abort, err)) break;
+            tc_fence_after();
+#pragma unroll 1
+            for (int L = kLevels - 1; L >= 0; --L) {
+                const float sc = ldexpf(1.0f, -kDigitBits * L);
+#pragma unroll
+                for (int half = 0; half < BN / 32; ++half) {
+                    float v[32];
+                    tc_ld32(lane_addr + static_cast<uint32_t>(L * BN + half * 32), v);
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) two_sum_into(h[half * 32 + j], l[half * 32 + j], v[j] * sc);
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&sh->accempty);
+#pragma unroll
+            for (int j = 0; j < BN; ++j) {
+                const float s = h[j] + l[j];
+                l[j] = l[j] - (s - h[j]);
+                h[j] = s;
+            }
+        }
+        if (!*abort) {
+            const int64_t gi = I * BM + q * 32 + lane;
+            store_row(out_h, out_l, ld, M, gi, J * BN, h, l, *scale_dev, accumulate);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    }
+}
+
+// The largest sqrt(w_k) = 1 / |sigma_k| as the bits of a positive double (they order as integers).
+__global__ void max_inv_sigma_kernel(const double* __restrict__ sigma, int64_t K,
+                                     unsigned long long* __restrict__ max_bits) {
+    unsigned long long m = 0;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < K; k += (int64_t)gridDim.x * blockDim.x) {
+        const double v = 1.0 / fabs(sigma[k]);
+        const unsigned long long b = (v == v && v < INFINITY) ? __double_as_longlong(v) : 0ull;
+        m = b > m ? b : m;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long x = __shfl_xor_sync(0xffffffffu, m, o);
+        m = x > m ? x : m;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(max_bits, m);
+}
+
+// s = 2^e >= max sqrt(w); the product's scale s^2 2^-(2 kFirstBits) as a float.
+__global__ void digit_scale_kernel(const unsigned long long* __restrict__ max_bits, int* __restrict__ e_out,
+                                   float* __restrict__ scale_out) {
+    const double m = __longlong_as_double(static_cast<long long>(*max_bits));
+    int e = 0;
+    if (m > 0.0) {
+        const double f = frexp(m, &e);  // m = f 2^e, f in [0.5, 1): 2^e > m
+        if (f == 0.5) e -= 1;            // m is a power of two: s = m
+    }
+    *e_out = e;
+    *scale_out = ldexpf(1.0f, 2 * e - 2 * kFirstBits);
+}
+
+// Digits of y = sqrt(w_k) {cos, sin}(2 pi t_ik) / s: D[d][i][kk] (cos) and D[d][i][kc + kk] (sin)
+// for k = k0 + kk; zero for k >= K or i >= M (padding).  Phase and sincospi in float64, digits
+// by exact float64 steps.
+__global__ void wtilde_digits_kernel(const double* __restrict__ sigma, const double* __restrict__ uv,
+                                     const double* __restrict__ grid, int64_t K, int64_t M, int64_t k0, int64_t kc,
+                                     int64_t Mp, const int* __restrict__ e_dev, __nv_bfloat16* __restrict__ D) {
+    const int64_t kk = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (kk >= kc) return;
+    const int64_t k = k0 + kk;
+    for (int64_t i = blockIdx.y; i < Mp; i += gridDim.y) {
+    double yc = 0.0, ys = 0.0;
+    if (k < K && i < M) {
+        const double u = uv[2 * k], v = uv[2 * k + 1];
+        const double t = fma(grid[2 * i + 1], u, grid[2 * i] * v);
+        const double sw = 1.0 / fabs(sigma[k]);
+        double sd, cd;
+        sincospi(2.0 * t, &sd, &cd);
+        const int e = *e_dev;
+        yc = ldexp(cd * sw, kFirstBits - e);
+        ys = ldexp(sd * sw, kFirstBits - e);
+    }
+    const int64_t Rc = 2 * kc;
+    const int64_t plane = Mp * Rc;
+    __nv_bfloat16* dc = D + i * Rc + kk;
+    __nv_bfloat16* ds = dc + kc;
+#pragma unroll
+    for (int d = 0; d < kDigits; ++d) {
+        const double qc = rint(yc), qs = rint(ys);
+        dc[d * plane] = __float2bfloat16_rn(static_cast<float>(qc));
+        ds[d * plane] = __float2bfloat16_rn(static_cast<float>(qs));
+        yc = (yc - qc) * (double)(1 << kDigitBits);
+        ys = (ys - qs) * (double)(1 << kDigitBits);
+    }
+    }
+}
+
+__global__ void poison_on_error_kernel(const int* __restrict__ err, float* __restrict__ out) {
+    if (*err) out[0] = __int_as_float(0x7fc00000);
+}
+
+// ------------------------------------------------------------------ host
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static std::mutex mu;
+    static EncodeTiledFn fn = nullptr;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+// the [kDigits][Mp][Rc] bf16 panel seen as boxes of {BK k, rows, kDigits}
+int make_map(CUtensorMap* map, const void* D, int64_t Rc, int64_t Mp, int rows) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return AJ_ERR_CUDA;
+    const cuuint64_t dims[3] = {static_cast<cuuint64_t>(Rc), static_cast<cuuint64_t>(Mp), kDigits};
+    const cuuint64_t strides[2] = {static_cast<cuuint64_t>(Rc) * 2, static_cast<cuuint64_t>(Mp * Rc) * 2};
+    const cuuint32_t box[3] = {BK, static_cast<cuuint32_t>(rows), kDigits};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(D), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? AJ_OK : AJ_ERR_CUDA;
+}
+
+int set_smem_attr() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return AJ_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev >= 0 && dev < 64 && done[dev]) return AJ_OK;
+    if (cudaFuncSetAttribute(digit_syrk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(kSmemBytes)) != cudaSuccess)
+        return AJ_ERR_CUDA;
+    if (dev >= 0 && dev < 64) done[dev] = true;
+    return AJ_OK;
+}
+
+int launch_syrk(const void* D, int64_t Rc, int64_t M, int64_t Mp, float* oh, float* ol, int64_t ld,
+                const float* scale_dev, int accumulate, int* err, cudaStream_t st) {
+    if (Rc <= 0 || Rc % kGroupRows != 0 || Mp % BM != 0 || Mp < M) return AJ_ERR_ARG;
+    if (reinterpret_cast<uintptr_t>(D) % 16 != 0) return AJ_ERR_ARG;
+    CUtensorMap ma, mb;
+    AJ_TRY(make_map(&ma, D, Rc, Mp, BM));
+    AJ_TRY(make_map(&mb, D, Rc, Mp, BN));
+    AJ_TRY(set_smem_attr());
+    const int64_t nI = Mp / BM;
+    const int64_t tiles = nI * (nI + 1);
+    digit_syrk_kernel<<<static_cast<unsigned>(tiles), kThreads, kSmemBytes, st>>>(ma, mb, Rc, M, oh, ol, ld, scale_dev,
+                                                                                 accumulate, err);
+    return check_launch();
+}
+
+}  // namespace tc
+
+// ------------------------------------------------ the mixed direct w_tilde
+
+struct WtildeTcPlan {
+    int64_t Mp, kc, Rc, nchunk;
+    size_t digit_bytes;
+};
+
+WtildeTcPlan wtilde_tc_plan(int64_t K, int64_t M) {
+    WtildeTcPlan p;
+    p.Mp = (M + tc::BM - 1) / tc::BM * tc::BM;
+    if (p.Mp == 0) p.Mp = tc::BM;
+    // visibilities a chunk: the panel ([digits][Mp][2 kc] bf16) within 2 GiB, kc a multiple of half a group
+    // (chunks of equal size, so the last one is not mostly padding)
+    const int64_t half = tc::kGroupRows / 2;
+    int64_t kmax = static_cast<int64_t>((size_t(2) << 30) / (size_t(tc::kDigits) * p.Mp * 2 * 2));
+    kmax = kmax / half * half;
+    if (kmax < half) kmax = half;
+    const int64_t Kpos = K > 0 ? K : 1;
+    p.nchunk = (Kpos + kmax - 1) / kmax;
+    const int64_t per = (Kpos + p.nchunk - 1) / p.nchunk;
+    p.kc = (per + half - 1) / half * half;
+    p.Rc = 2 * p.kc;
+    p.digit_bytes = size_t(tc::kDigits) * p.Mp * p.Rc * 2;
+    return p;
+}
+
+size_t wtilde_tc_workspace_bytes(int64_t K, int64_t M) {
+    WtildeTcPlan p = wtilde_tc_plan(K, M);
+    Sizer s;
+    s.take<char>(p.digit_bytes);
+    s.take<unsigned long long>(1);
+    s.take<int>(2);
+    s.take<float>(1);
+    return s.total();
+}
+
+// ph/pl (M x M, leading dimension M) receive the lower triangle of W as double-float planes.
+int wtilde_tc(const double* sigma, const double* uv, const double* grid, int64_t K, int64_t M, float* ph, float* pl,
+              void* ws, size_t bytes, cudaStream_t st) {
+    WtildeTcPlan p = wtilde_tc_plan(K, M);
+    if (bytes < wtilde_tc_workspace_bytes(K, M)) return AJ_ERR_WORKSPACE;
+    Carver cv(ws, bytes);
+    auto* D = cv.take<__nv_bfloat16>(p.digit_bytes / 2);
+    auto* maxbits = cv.take<unsigned long long>(1);
+    int* ints = cv.take<int>(2);  // [0] the scale exponent, [1] the error word
+    float* scale = cv.take<float>(1);
+    if (cudaMemsetAsync(maxbits, 0, sizeof(unsigned long long), st) != cudaSuccess ||
+        cudaMemsetAsync(ints, 0, 2 * sizeof(int), st) != cudaSuccess)
+        return AJ_ERR_CUDA;
+    tc::max_inv_sigma_kernel<<<blocks_for(K, 256, 4 * num_sms()), 256, 0, st>>>(sigma, K, maxbits);
+    AJ_LAUNCHED();
+    tc::digit_scale_kernel<<<1, 1, 0, st>>>(maxbits, ints, scale);
+    AJ_LAUNCHED();
+    for (int64_t ch = 0; ch < p.nchunk; ++ch) {
+        dim3 g(static_cast<unsigned>((p.kc + 255) / 256), static_cast<unsigned>(p.Mp < 65535 ? p.Mp : 65535));
+        tc::wtilde_digits_kernel<<<g, 256, 0, st>>>(sigma, uv, grid, K, M, ch * p.kc, p.kc, p.Mp, ints, D);
+        AJ_LAUNCHED();
+        AJ_TRY(tc::launch_syrk(D, p.Rc, M, p.Mp, ph, pl, M, scale, ch > 0 ? 1 : 0, ints + 1, st));
+    }
+    tc::poison_on_error_kernel<<<1, 1, 0, st>>>(ints + 1, ph);
+    return check_launch();
+}
+
+}  // namespace aj
+
+using namespace aj;
+
+extern "C" {
+
+int aj_digit_syrk_probe(const void* digits, int64_t rows, int64_t M, float* out_hi, float* out_lo,
+                        const float* scale, int accumulate, int* err, void* stream) {
+    if (!digits || !out_hi || !out_lo || !scale || !err || M <= 0 || rows <= 0) return AJ_ERR_ARG;
+    const int64_t Mp = (M + tc::BM - 1) / tc::BM * tc::BM;
+    return tc::launch_syrk(digits, rows, M, Mp, out_hi, out_lo, M, scale, accumulate, err, as_stream(stream));
+}
+
+}  // extern "C"

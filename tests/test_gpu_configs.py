@@ -14,8 +14,10 @@ gathers (M > 1,024) and the multi-panel factorisations (S > 1,024 at K = 1e6).
   oracle's own M x M sum over 1e6 visibilities would take hours on the host).
 
 Tolerances: float64 path rel 1e-10 (entries that cancel judged against 1e-11 of
-the result's scale); s against cond(A) as in the golden solve test; the mixed
-path as each test states.
+the result's scale); logE where A is so ill-conditioned (cond ~1e13 at lambda =
+1e-3) that LAPACK's LU and Cholesky of the same float64 A already disagree by
+more than that, within 4x their disagreement; s against cond(A) as in the
+golden solve test; the mixed path as each test states.
 """
 
 from __future__ import annotations
@@ -131,8 +133,26 @@ def test_fp64_solve_matches_oracle(cfg, lam):
     assert res < 1e-13, res
 
 
+def _lapack_spread(d, F, H, D):
+    """|logE by LU - logE by Cholesky| on the same float64 inputs: how closely two LAPACK
+    factorisations of A agree at its conditioning (the float64 noise floor of logE)."""
+    import scipy.linalg as sl
+
+    r_lu = ref._evidence(d["noise_map"], d["data"], F, H, D)
+    A = F + H
+    ca = sl.cho_factor(A, lower=True)
+    ch = sl.cho_factor(H, lower=True)
+    s = sl.cho_solve(ca, D)
+    chi = np.ascontiguousarray(d["data"]).view(np.float64) / np.ascontiguousarray(d["noise_map"]).view(np.float64)
+    r_ch = -0.5 * (chi @ chi - s @ D + 2 * np.log(np.diag(ca[0])).sum() - 2 * np.log(np.diag(ch[0])).sum()
+                   + ref.noise_normalization_complex_from(d["noise_map"]))
+    return abs(r_lu - r_ch)
+
+
 @pytest.mark.parametrize("lam", LAMBDAS)
 def test_fp64_log_evidence_matches_oracle(cfg, lam):
+    """logE at rel 1e-10, or, where A's conditioning puts two LAPACK factorisations of the same
+    float64 A further apart than that (cond ~1e13 at lambda = 1e-3), within 4x their spread."""
     import autojax_gb300 as aj
 
     d = cfg["d"]
@@ -142,13 +162,15 @@ def test_fp64_log_evidence_matches_oracle(cfg, lam):
     logE, dlam, gw, s = float(logE), float(dlam), gw.cpu().numpy(), s.cpu().numpy()
     a = _args(d, cfg["W"])
     r_logE, r_dlam, r_gw = adjoint.log_evidence_and_grad(*a, coefficient=c)
-    assert abs(logE - r_logE) <= RTOL * abs(r_logE), (logE, r_logE)
-    plain = ref.log_likelihood_function_via_w_tilde_from(*a, coefficient=c)
-    assert abs(logE - plain) <= RTOL * abs(plain), (logE, plain)
-    # s, dlogE/dlambda and the weight gradient go through A^-1: judged against cond(A)
     H = ref.constant_regularization_matrix_from(c, d["neighbors"], d["neighbors_sizes"])
-    A = ref.curvature_matrix_via_w_tilde_from(cfg["W"], cfg["T"]) + H
+    F = ref.curvature_matrix_via_w_tilde_from(cfg["W"], cfg["T"])
     D = ref.data_vector_from(cfg["T"], d["dirty_image"])
+    tol = max(RTOL * abs(r_logE), 4.0 * _lapack_spread(d, F, H, D))
+    assert abs(logE - r_logE) <= tol, (logE, r_logE, tol)
+    plain = ref.log_likelihood_function_via_w_tilde_from(*a, coefficient=c)
+    assert abs(logE - plain) <= tol, (logE, plain)
+    # s, dlogE/dlambda and the weight gradient go through A^-1: judged against cond(A)
+    A = F + H
     ev = np.linalg.eigvalsh(A)
     cond = ev[-1] / ev[0]
     s_ref = np.linalg.solve(A, D)
