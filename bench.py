@@ -302,6 +302,14 @@ def roofline(A, dist: Dist, tune_policy: bool = True):
     finally:
         tune.set_tile_policy(*saved)
     t_inv_fp64 = time_region(inv_fp64, reps, dist, "roofline_fp64") / reps
+
+    # the same float64 work through the vendor's solver (torch.linalg: cuSOLVER/MAGMA), for scale
+    def inv_vendor(i):
+        L, _ = torch.linalg.cholesky_ex(A)
+        torch.cholesky_inverse(L)
+
+    inv_vendor(0)
+    t_inv_vendor = time_region(inv_vendor, reps, dist, "roofline_fp64_vendor") / reps
     fp64_peak = fma_peak_tflops(_lib.AJ_FP64)
     fp32_peak = fma_peak_tflops(_lib.AJ_MIXED)
     df_peak = fp32_peak / 11.4
@@ -323,6 +331,9 @@ def roofline(A, dist: Dist, tune_policy: bool = True):
         "ms": 1e3 * t_inv_mixed,
         "fp64_same_work_ms": 1e3 * t_inv_fp64,
         "fp64_same_work_frac_of_fp64_peak": inv_flops / t_inv_fp64 / 1e12 / fp64_peak,
+        "fp64_vendor_same_work_ms": 1e3 * t_inv_vendor,
+        "fp64_vendor_note": "torch.linalg.cholesky_ex + torch.cholesky_inverse in float64 on the same A "
+                            "(the vendor solver, not this library): a reference point for the float64 path",
     }
     # the same launch against the measured peaks (neither bounds a float32-pipe group)
     mp = measured_peaks()

@@ -42,6 +42,7 @@ extern "C" {
 #define AJ_INFO_OK 0
 #define AJ_INFO_INDEX_RANGE 1       /* an index was outside [0, n) and not -1 */
 #define AJ_INFO_NOT_POSITIVE_DEFINITE 2 /* Cholesky met a pivot <= 0 or NaN */
+#define AJ_INFO_SINGULAR 3              /* LU met an exactly zero (or NaN) pivot */
 
 #define AJ_FP64 0
 #define AJ_MIXED 1
@@ -227,8 +228,9 @@ int aj_constant_regularization(double coefficient, const int64_t* neighbors, con
                                int64_t S, int64_t P, double* out, int* info, void* stream);
 
 /* numba.py:699-731 reconstruction_positive_negative_from: out (S,) = A^-1 D by
- * a blocked FP64 Cholesky (A symmetric positive definite; the reference's LU
- * also accepts indefinite A — here such A sets AJ_INFO_NOT_POSITIVE_DEFINITE). */
+ * a blocked FP64 Cholesky (A symmetric positive definite; an indefinite A sets
+ * AJ_INFO_NOT_POSITIVE_DEFINITE, and aj_lu_solve then solves it as the
+ * reference's LU does). */
 size_t aj_spd_solve_workspace_size(int64_t S);
 int aj_spd_solve(const double* data_vector, const double* A, int64_t S, double* out, void* workspace,
                  size_t workspace_bytes, int* info, void* stream);
@@ -248,6 +250,15 @@ int aj_spd_solve(const double* data_vector, const double* A, int64_t S, double* 
  * All calls in a context share the array: calls whose GPU work overlaps race. */
 #define AJ_NOALLOC_SOLVE_MAX_S 1024
 int aj_spd_solve_noalloc(const double* data_vector, const double* A, int64_t S, double* out, int* info, void* stream);
+
+/* numba.py:731 np.linalg.solve and numba.py:849-850 np.linalg.slogdet(...)[1] for
+ * any non-singular A: blocked float64 LU with partial pivoting (the first row of
+ * largest magnitude, as LAPACK getrf). out (S,) = A^-1 D and *logabsdet =
+ * log|det A|, either may be NULL; an exactly zero pivot sets AJ_INFO_SINGULAR
+ * (the reference raises LinAlgError there). */
+size_t aj_lu_solve_workspace_size(int64_t S);
+int aj_lu_solve(const double* data_vector, const double* A, int64_t S, double* out, double* logabsdet,
+                void* workspace, size_t workspace_bytes, int* info, void* stream);
 
 /* log|det A| of a symmetric positive definite A (the slogdet of numba.py:849-850). */
 int aj_spd_logdet(const double* A, int64_t S, double* out, void* workspace, size_t workspace_bytes, int* info,

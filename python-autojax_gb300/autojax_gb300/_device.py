@@ -97,6 +97,8 @@ class Call:
             raise IndexError(f"{self.name}: index out of range (flat position {where})")
         if code == _lib.AJ_INFO_NOT_POSITIVE_DEFINITE:
             raise np.linalg.LinAlgError(f"{self.name}: matrix is not positive definite (pivot {where})")
+        if code == _lib.AJ_INFO_SINGULAR:
+            raise np.linalg.LinAlgError(f"{self.name}: Singular matrix (zero pivot {where})")
 
     def out(self, t: torch.Tensor):
         return t.cpu().numpy() if self.numpy_out else t

@@ -21,6 +21,7 @@ AJ_NOALLOC_SOLVE_MAX_S = 1024
 AJ_BATCH_BRANCHES = 16
 AJ_INFO_INDEX_RANGE = 1
 AJ_INFO_NOT_POSITIVE_DEFINITE = 2
+AJ_INFO_SINGULAR = 3
 AJ_FP64 = 0
 AJ_MIXED = 1
 
@@ -95,6 +96,8 @@ SIGNATURES = {
     "aj_spd_solve_workspace_size": (SZ, [I64]),
     "aj_spd_solve": (INT, [P, P, I64, P, P, SZ, P, P]),
     "aj_spd_solve_noalloc": (INT, [P, P, I64, P, P, P]),
+    "aj_lu_solve_workspace_size": (SZ, [I64]),
+    "aj_lu_solve": (INT, [P, P, I64, P, P, P, SZ, P, P]),
     "aj_spd_logdet": (INT, [P, I64, P, P, SZ, P, P]),
     "aj_spd_inverse_workspace_size": (SZ, [I64]),
     "aj_spd_inverse": (INT, [P, I64, P, P, P, SZ, P, P]),

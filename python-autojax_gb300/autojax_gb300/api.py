@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import math
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -358,8 +359,25 @@ def constant_regularization_matrix_from(coefficient, neighbors, neighbors_sizes)
     return c.out(out)
 
 
+def _lu_solve(c: Call, D, A, S, want_solution=True):
+    """x = A^-1 D and log|det A| by the float64 LU with partial pivoting (numba.py:731, 849-850)."""
+    out = c.empty(S) if want_solution else None
+    logabsdet = c.empty(1)
+    ws = c.workspace(_lib.load().aj_lu_solve_workspace_size(S))
+    info = c.info()
+    _lib_call("aj_lu_solve", ptr(D), ptr(A), S, ptr(out), ptr(logabsdet), ptr(ws), ws.numel(), ptr(info), c.stream())
+    c.check_info(info)
+    return out, logabsdet
+
+
 def reconstruction_positive_negative_from(data_vector, curvature_reg_matrix):
-    """numba.py:699-731 — s = A^-1 D by a float64 Cholesky solve (A symmetric positive definite)."""
+    """numba.py:699-731 — s = A^-1 D.
+
+    A float64 Cholesky solve; an A that is not positive definite (which the
+    inversion's A = F + H never is, but a caller's matrix may be) is solved by
+    the LU with partial pivoting the reference's np.linalg.solve uses, and a
+    singular one raises LinAlgError as there.
+    """
     c = Call("reconstruction_positive_negative_from")
     D = c.arr(data_vector, f64, 1, "data_vector")
     A = c.arr(curvature_reg_matrix, f64, 2, "curvature_reg_matrix")
@@ -368,6 +386,9 @@ def reconstruction_positive_negative_from(data_vector, curvature_reg_matrix):
     ws = c.workspace(_lib.load().aj_spd_solve_workspace_size(S))
     info = c.info()
     _lib_call("aj_spd_solve", ptr(D), ptr(A), S, ptr(out), ptr(ws), ws.numel(), ptr(info), c.stream())
+    if int(info[0].item()) == _lib.AJ_INFO_NOT_POSITIVE_DEFINITE:
+        out, _ = _lu_solve(c, D, A, S)
+        return c.out(out)
     c.check_info(info)
     return c.out(out)
 
@@ -425,25 +446,66 @@ def _evidence(c: Call, p, precision, with_grad):
     return out, gw, rec
 
 
+def _evidence_by_lu(c: Call, F, dirty_image, data, noise_map, pix_indexes, pix_weights, neighbors, neighbors_sizes,
+                    coefficient):
+    """numba.py:839-857 assembled from the library's entry points with both log|det| and the solve
+    by LU: the fallback for an A = F + H that is not positive definite (float64 throughout)."""
+    S = int(c.arr(neighbors_sizes, i64, 1, "neighbors_sizes").shape[0])
+    Fd = c.arr(F, f64, 2, "curvature_matrix")
+    H = c.arr(constant_regularization_matrix_from(coefficient, c.arr(neighbors, i64, 2, "neighbors"),
+                                                  c.arr(neighbors_sizes, i64, 1, "neighbors_sizes")), f64, 2, "H")
+    A = (Fd + H).contiguous()
+    T = mapping_matrix_from(c.arr(pix_indexes, i64, 2, "pix_indexes_for_sub_slim_index"),
+                            c.arr(pix_weights, f64, 2, "pix_weights_for_sub_slim_index"), S)
+    D = data_vector_from(T, c.arr(dirty_image, f64, 1, "dirty_image"))
+    s, log_a = _lu_solve(c, D, A, S)
+    _, log_h = _lu_solve(c, None, H, S, want_solution=False)
+    da = c.complex_as_real(data, "data").reshape(-1)
+    nm = c.complex_as_real(noise_map, "noise_map").reshape(-1)
+    chi = da / nm
+    norm = noise_normalization_complex_from(c.arr(noise_map, torch.complex128, 1, "noise_map"))
+    return -0.5 * (chi @ chi - s @ D + log_a[0] - log_h[0] + norm)
+
+
 def log_likelihood_function_via_w_tilde_from(dirty_image, data, noise_map, w_tilde, pix_indexes_for_sub_slim_index,
                                              pix_weights_for_sub_slim_index, neighbors, neighbors_sizes, *,
                                              coefficient=1.0, precision="fp64"):
-    """numba.py:761-857 — the log-evidence with a dense w_tilde."""
+    """numba.py:761-857 — the log-evidence with a dense w_tilde.
+
+    An A = F + H that is not positive definite falls back to the reference's
+    LU semantics (solve and log|det| by LU, float64), see _evidence_by_lu.
+    """
     c = Call("log_likelihood_function_via_w_tilde_from")
     p = _problem(c, dirty_image, data, noise_map, pix_indexes_for_sub_slim_index, pix_weights_for_sub_slim_index,
                  neighbors, neighbors_sizes, coefficient, w_tilde=w_tilde)
-    out, _, _ = _evidence(c, p, precision, False)
+    try:
+        out, _, _ = _evidence(c, p, precision, False)
+    except np.linalg.LinAlgError:
+        T = mapping_matrix_from(c.arr(pix_indexes_for_sub_slim_index, i64, 2, "pix_indexes_for_sub_slim_index"),
+                                c.arr(pix_weights_for_sub_slim_index, f64, 2, "pix_weights_for_sub_slim_index"),
+                                int(p.S))
+        F = curvature_matrix_via_w_tilde_from(c.arr(w_tilde, f64, 2, "w_tilde"), T)
+        return c.scalar(_evidence_by_lu(c, F, dirty_image, data, noise_map, pix_indexes_for_sub_slim_index,
+                                        pix_weights_for_sub_slim_index, neighbors, neighbors_sizes, coefficient))
     return c.scalar(out[0])
 
 
 def log_likelihood_function_via_w_compact_from(dirty_image, data, noise_map, w_compact, native_index_for_slim_index,
                                                pix_indexes_for_sub_slim_index, pix_weights_for_sub_slim_index,
                                                neighbors, neighbors_sizes, *, coefficient=1.0, precision="fp64"):
-    """numba.py:866-967 — the log-evidence from the compact table."""
+    """numba.py:866-967 — the log-evidence from the compact table (LU fallback as above)."""
     c = Call("log_likelihood_function_via_w_compact_from")
     p = _problem(c, dirty_image, data, noise_map, pix_indexes_for_sub_slim_index, pix_weights_for_sub_slim_index,
                  neighbors, neighbors_sizes, coefficient, w_compact=w_compact, native_index=native_index_for_slim_index)
-    out, _, _ = _evidence(c, p, precision, False)
+    try:
+        out, _, _ = _evidence(c, p, precision, False)
+    except np.linalg.LinAlgError:
+        F = curvature_matrix_via_w_compact_sparse_mapping_matrix_from(
+            c.arr(w_compact, f64, 2, "w_compact"), c.arr(native_index_for_slim_index, i64, 2, "native_index"),
+            c.arr(pix_indexes_for_sub_slim_index, i64, 2, "pix_indexes_for_sub_slim_index"),
+            c.arr(pix_weights_for_sub_slim_index, f64, 2, "pix_weights_for_sub_slim_index"), int(p.S))
+        return c.scalar(_evidence_by_lu(c, F, dirty_image, data, noise_map, pix_indexes_for_sub_slim_index,
+                                        pix_weights_for_sub_slim_index, neighbors, neighbors_sizes, coefficient))
     return c.scalar(out[0])
 
 

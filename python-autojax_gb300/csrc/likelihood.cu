@@ -587,6 +587,23 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
             cudaStreamWaitEvent(st, ln.ev[kEvPreDone], 0);
             return rc;
         }
+        if (!mixed) {
+            // H's float64 chain beside A's on lane 5: the factor, then (with the gradient) L^-1 and
+            // tr(H^-1)'s partial sums; A's factor, solve and inverse stay on this stream
+            cudaStream_t hlane = ln.s[5];
+            if (cudaStreamWaitEvent(hlane, ln.ev[kEvHReady], 0) != cudaSuccess) return AJ_ERR_CUDA;
+            rc = spd_factor(b.H, S, b.wh, b.logdets + 1, info, hlane);
+            if (rc == AJ_OK && with_grad) rc = spd_invert_factor(S, b.wh, info, hlane);
+            if (rc == AJ_OK && with_grad) {
+                frob_lower_kernel<<<(unsigned)b.nfrob, 256, 0, hlane>>>(b.wh.Linv, S, b.fpart);
+                rc = check_launch();
+            }
+            if (cudaEventRecord(ln.ev[kEvHDone], hlane) != cudaSuccess) return AJ_ERR_CUDA;
+            if (rc != AJ_OK) {
+                cudaStreamWaitEvent(st, ln.ev[kEvHDone], 0);
+                return rc;
+            }
+        }
         if (mixed) {
             // H's factorisation (and, with the gradient, its L^-1 for tr(H^-1)) beside A's, from
             // lane 5 (which A's factorisation never forks or joins), on lanes of its own
@@ -622,7 +639,6 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         add_kernel<<<blocks_for(S * S, 256, 8 * num_sms()), 256, 0, st>>>(b.F, b.H, b.A, S * S);
         AJ_LAUNCHED();
         AJ_TRY(spd_factor(b.A, S, b.wa, b.logdets + 0, info, st));
-        AJ_TRY(spd_factor(b.H, S, b.wh, b.logdets + 1, info, st));
         AJ_TRY(spd_solve_vec(S, b.wa, b.D, b.s, info, st));
     } else {
         // the same chain in double-float on the float32 pipe
@@ -664,8 +680,9 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         AJ_TRY(dfspd_solve_refined(S, b.da, b.Ah, b.Al, b.D, b.s, st, with_grad ? b.AIh : nullptr,
                                    with_grad ? b.AIl : nullptr, true, with_grad ? b.sh : nullptr,
                                    with_grad ? b.sl : nullptr));
-        if (cudaStreamWaitEvent(st, ln.ev[kEvHDone], 0) != cudaSuccess) return AJ_ERR_CUDA;
     }
+    // H's chain (log|H|, and tr(H^-1)'s partial sums with the gradient) joins before the assembly
+    if (cudaStreamWaitEvent(st, ln.ev[kEvHDone], 0) != cudaSuccess) return AJ_ERR_CUDA;
 
     // logE from the chi^2 and log-noise sums (side lane), s.D and the log-determinants; on the
     // mixed path with the gradient it runs on the side lane beside the weight gradient
@@ -684,9 +701,6 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
     if (!mixed) {
         AJ_TRY(spd_invert_factor(S, b.wa, info, st));
         AJ_TRY(spd_inverse_from_factor(S, b.wa, b.Ainv, st));
-        AJ_TRY(spd_invert_factor(S, b.wh, info, st));
-        frob_lower_kernel<<<(unsigned)b.nfrob, 256, 0, st>>>(b.wh.Linv, S, b.fpart);
-        AJ_LAUNCHED();
     }
     // dlogE/dlambda (and, mixed, the assembly) on the side lane while st computes the weight
     // gradient; both read only finished data

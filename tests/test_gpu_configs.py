@@ -215,3 +215,28 @@ def test_mixed_matches_oracle(cfg, lam):
     trace_scale = d["S"] / lam
     assert abs(dlam - r_dlam) <= 1e-6 * trace_scale + 1e-5 * abs(r_dlam), (dlam, r_dlam)
     np.testing.assert_allclose(gw, r_gw, rtol=0, atol=max(1e-5, 2e-15 * cond) * np.abs(r_gw).max())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_compact_table_route_matches_at_size(cfg, precision):
+    """The low-memory route (F from the N x (2N-1) offset table, W~ never stored; numba.py:439-653,
+    866-967) against the dense-W~ route on the same table, at the configuration's M."""
+    import torch
+
+    import autojax_gb300 as aj
+
+    d = cfg["d"]
+    dev = cfg["Wd"].device
+    n = torch.from_numpy(d["noise_map_real"]).to(dev)
+    uv = torch.from_numpy(d["uv_wavelengths"]).to(dev)
+    wc = aj.w_compact_curvature_interferometer_from(d["grid_size"], n, uv, d["pixel_scale"])
+    nat = torch.from_numpy(d["native_index_for_slim_index"]).to(dev)
+    a = _args(d, cfg["Wd"])
+    c = 1.0
+    dense = float(aj.log_likelihood_function_via_w_tilde_from(*a, coefficient=c, precision=precision))
+    compact = float(aj.log_likelihood_function_via_w_compact_from(a[0], a[1], a[2], wc, nat, *a[4:], coefficient=c,
+                                                                  precision=precision))
+    tol = 1e-10 if precision == "fp64" else 1e-8
+    assert abs(compact - dense) <= tol * abs(dense), (compact, dense)
+    exp = ref.log_likelihood_function_via_w_tilde_from(*_args(d, cfg["W"]), coefficient=c)
+    assert abs(compact - exp) <= (1e-10 if precision == "fp64" else 1e-7) * abs(exp), (compact, exp)
