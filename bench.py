@@ -573,20 +573,21 @@ def batched_bench(args, dev, dist: Dist) -> dict:
     }
 
 
-def wtilde_bench(d, dev, fp32_peak) -> dict:
+def wtilde_bench(d, dev, fp32_peak, Ks: int = 65536) -> dict:
     """Direct w_tilde build (numba.py:156-207) on the workload's M with a visibility sample.
 
-    The mixed build does 2 double-float multiply-adds per unique (pixel pair,
-    visibility) term, 11.4 float32 instructions each; `fp32_pipe_frac` is the
-    float32 FMA-pipe share those instructions imply (ncu's pipe counters for
-    the same kernel are in the profiles).
+    The mixed build cuts the float64 panel into 7 exact 7-bit digits and sums the 28 digit pairs
+    of levels 0..6 on the bf16 tensor cores: 2 x 28 digit multiply-adds (112 bf16 flops) per unique
+    (pixel pair, visibility) term of the computed tiles.  Reported against the measured bf16 peak,
+    and under the fixed convention of 20 float32 flops a term (phase, cos, Kahan accumulate)
+    against the measured float32 FMA rate, the unit the w_tilde target is stated in.
     """
     import torch
 
     from autojax_gb300 import _lib
 
     lib = _lib.load()
-    Ks = 8192
+    Ks = min(Ks, d["K"])
     g = torch.from_numpy(d["grid_radians_slim"]).to(dev)
     uv = torch.from_numpy(d["uv_wavelengths"][:Ks].copy()).to(dev)
     n = torch.from_numpy(d["noise_map_real"][:Ks].copy()).to(dev)
@@ -611,15 +612,24 @@ def wtilde_bench(d, dev, fp32_peak) -> dict:
     e1.synchronize()
     sec = e0.elapsed_time(e1) / 1e3
     terms = M * (M + 1) / 2 * Ks
-    fp32_flops = terms * 2 * 11.4 * 2
+    Mp = (M + 127) // 128 * 128
+    tile_terms = (Mp // 128) * (Mp // 128 + 1) * 128 * 64 * Ks  # the computed tiles' (pair, visibility) terms
+    bf16_tflops = tile_terms * 112 / sec / 1e12
+    mp = measured_peaks()
     rng = np.random.default_rng(17)
     rows = np.repeat(np.array([0, M // 3, M // 2, M - 1]), 64)
     cols = rng.integers(0, M, rows.size)
     cols[::64] = rows[::64]
     Wh = W.cpu().numpy()
-    return {"precision": "mixed (float64 panel, double-float product)", "K_sample": Ks, "M": M, "seconds": sec,
-            "terms_per_s": terms / sec, "fp32_pipe_frac": fp32_flops / sec / 1e12 / fp32_peak,
-            "fp32_pipe_frac_note": "double-float arithmetic only (22.8 float32 instructions per term)",
+    return {"precision": "mixed: float64 panel cut into 7 exact 7-bit digits, digit products on the bf16 tensor "
+                         "cores (tcgen05), folded into double-float",
+            "K_sample": Ks, "M": M, "seconds": sec, "terms_per_s": terms / sec,
+            "fp32_convention_frac": terms / sec * 20 / 1e12 / fp32_peak,
+            "fp32_convention_note": "unique terms x 20 float32 flops a term over the measured float32 FMA rate",
+            "tensor_tflops": bf16_tflops,
+            "bf16_tensor_frac": bf16_tflops / mp["bf16_tflops"] if mp.get("bf16_tflops") else None,
+            "tensor_note": "112 bf16 flops (2 rows x 28 digit pairs) per term of the computed 128 x 64 tiles, "
+                           "over MEASURED_PEAKS.json's bf16 burst peak",
             "sample": {"rows": rows, "cols": cols, "values": Wh[rows, cols],
                        "noise": d["noise_map_real"][:Ks].copy(), "uv": d["uv_wavelengths"][:Ks].copy()}}
 

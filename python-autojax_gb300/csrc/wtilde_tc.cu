@@ -191,14 +191,31 @@ __device__ __forceinline__ uint64_t desc_sw64(uint32_t saddr) {
 // kind::f16 instruction descriptor: float32 accumulator, bf16 A and B, both K-major, M = 128, N = 64.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(BN >> 3) << 17) | (uint32_t(BM >> 4) << 24);
 
-// lower block-triangle tile t -> (row tile I of 128 rows, column tile J of 64 columns), J <= 2I + 1
-__device__ __forceinline__ void tile_of(int64_t t, int64_t& I, int64_t& J) {
-    // tiles before row I: I (I + 1)
-    int64_t r = static_cast<int64_t>((sqrt(4.0 * (double)t + 1.0) - 1.0) * 0.5);
-    while (r * (r + 1) > t) --r;
-    while ((r + 1) * (r + 2) <= t) ++r;
-    I = r;
-    J = t - r * (r + 1);
+// Lower block-triangle tile t -> (row tile I of 128 rows, column tile J of 64 columns), J <= 2I + 1.
+// Tiles go in bands of kBand row tiles, column-major inside a band, so the CTAs resident at once
+// share both operands' rows (a band's A rows and a run of B rows) in L2 instead of each reading a
+// B tile of its own.
+constexpr int64_t kBand = 8;
+__device__ __forceinline__ void tile_of(int64_t t, int64_t nI, int64_t& I, int64_t& J) {
+    int64_t i0 = 0;
+    for (;;) {
+        const int64_t i1 = min(nI, i0 + kBand);
+        const int64_t n = (i1 - i0) * (i0 + i1 + 1);  // sum over I in [i0, i1) of 2I + 2
+        if (t < n || i1 >= nI) break;
+        t -= n;
+        i0 = i1;
+    }
+    const int64_t i1 = min(nI, i0 + kBand);
+    for (int64_t j = 0;; ++j) {
+        const int64_t ilo = max(i0, j / 2);  // the rows of this band with 2I + 1 >= j
+        const int64_t cnt = i1 > ilo ? i1 - ilo : 0;
+        if (t < cnt) {
+            I = ilo + t;
+            J = j;
+            return;
+        }
+        t -= cnt;
+    }
 }
 
 __device__ __forceinline__ void two_sum_into(float& hi, float& lo, float c) {
@@ -240,14 +257,15 @@ __device__ __forceinline__ void store_row(float* __restrict__ oh, float* __restr
 // One CTA per lower tile; Rc rows of digits (a multiple of kGroupRows).  s2 = s^2 2^-(2 first bits).
 __global__ void __launch_bounds__(kThreads, 1)
     digit_syrk_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
-                      int64_t Rc, int64_t M, float* __restrict__ out_h, float* __restrict__ out_l, int64_t ld,
+                      int64_t Rc, int64_t M, int64_t Mp, float* __restrict__ out_h, float* __restrict__ out_l,
+                      int64_t ld,
                       const float* __restrict__ scale_dev, int accumulate, int* __restrict__ err) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     Shared* sh = reinterpret_cast<Shared*>(base + size_t(kStages) * kStageBytes);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int64_t I, J;
-    tile_of(blockIdx.x, I, J);
+    tile_of(blockIdx.x, Mp / BM, I, J);
     const int ngroups = static_cast<int>(Rc / kGroupRows);
     const int nstages = ngroups * kStagesPerGroup;
 
@@ -513,8 +531,8 @@ int launch_syrk(const void* D, int64_t Rc, int64_t M, int64_t Mp, float* oh, flo
     AJ_TRY(set_smem_attr());
     const int64_t nI = Mp / BM;
     const int64_t tiles = nI * (nI + 1);
-    digit_syrk_kernel<<<static_cast<unsigned>(tiles), kThreads, kSmemBytes, st>>>(ma, mb, Rc, M, oh, ol, ld, scale_dev,
-                                                                                 accumulate, err);
+    digit_syrk_kernel<<<static_cast<unsigned>(tiles), kThreads, kSmemBytes, st>>>(ma, mb, Rc, M, Mp, oh, ol, ld,
+                                                                                 scale_dev, accumulate, err);
     return check_launch();
 }
 

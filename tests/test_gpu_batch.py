@@ -224,3 +224,47 @@ def test_release_stream_frees_and_recreates_side_streams(setup):
     s.synchronize()
     np.testing.assert_array_equal(batch.out.cpu().numpy(), first)
     assert lib.aj_release_stream(s.cuda_stream) == _lib.AJ_OK
+
+
+def test_batch_at_the_batched_configuration_sizes_matches_oracle():
+    """Three members of a batch at the batched configuration's sizes (K = 5e5, M = 7,860 image
+    pixels, S = 500, 1,250 and 2,000), mixed precision with gradients, against the oracle on the
+    same shared w_tilde (the float64 table expansion the batch reads)."""
+    import torch
+
+    import autojax_gb300 as aj
+    from autojax_gb300 import synthetic
+    from autojax_gb300.inversion import Dataset, LogEvidenceBatch
+
+    d = synthetic.make_dataset("cfg5")
+    dev = torch.device("cuda", 0)
+    wc = aj.w_compact_curvature_interferometer_from(d["grid_size"], torch.from_numpy(d["noise_map_real"]).to(dev),
+                                                    torch.from_numpy(d["uv_wavelengths"]).to(dev), d["pixel_scale"])
+    Wd = aj.w_tilde_via_compact_from(wc, torch.from_numpy(d["native_index_for_slim_index"]).to(dev))
+    W = Wd.cpu().numpy()
+    models = [synthetic.lens_models(d, 1, S_range=(S, S), seed=70 + S)[0] for S in (500, 1250, 2000)]
+    ds = Dataset(d["dirty_image"], d["data"], d["noise_map"], Wd, precision="mixed", device=dev)
+    P = max(m["neighbors"].shape[1] for m in models)
+    batch = LogEvidenceBatch(ds, [m["S"] for m in models], B=3, P=P)
+    for i, m in enumerate(models):
+        batch.set_model(i, m["pix_indexes_for_sub_slim_index"], m["pix_weights_for_sub_slim_index"], m["neighbors"],
+                        m["neighbors_sizes"], m["coefficient"])
+    batch.launch()
+    torch.cuda.synchronize()
+    batch.check()
+    out = batch.out.cpu().numpy()
+    for i, m in enumerate(models):
+        r_logE, r_dlam, r_gw = adjoint.log_evidence_and_grad(
+            d["dirty_image"], d["data"], d["noise_map"], W, m["pix_indexes_for_sub_slim_index"],
+            m["pix_weights_for_sub_slim_index"], m["neighbors"], m["neighbors_sizes"], coefficient=m["coefficient"])
+        c = m["coefficient"]
+        assert abs(out[i, 0] - r_logE) <= 1e-7 * abs(r_logE), (m["S"], out[i, 0], r_logE)
+        assert abs(out[i, 1] - r_dlam) <= 1e-6 * m["S"] / c**2 + 1e-5 * abs(r_dlam), (m["S"], out[i, 1], r_dlam)
+        from oracle import numpy_port as ref
+
+        T = ref.mapping_matrix_from(m["pix_indexes_for_sub_slim_index"], m["pix_weights_for_sub_slim_index"], m["S"])
+        H = ref.constant_regularization_matrix_from(c, m["neighbors"], m["neighbors_sizes"])
+        ev = np.linalg.eigvalsh(T.T @ W @ T + H)
+        cond = ev[-1] / ev[0]
+        gw = batch.evals[i].grad_weights.cpu().numpy()
+        np.testing.assert_allclose(gw, r_gw, rtol=0, atol=max(1e-5, 2e-15 * cond) * np.abs(r_gw).max())
