@@ -592,8 +592,7 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
             // tr(H^-1)'s partial sums; A's factor, solve and inverse stay on this stream
             cudaStream_t hlane = ln.s[5];
             if (cudaStreamWaitEvent(hlane, ln.ev[kEvHReady], 0) != cudaSuccess) return AJ_ERR_CUDA;
-            rc = spd_factor(b.H, S, b.wh, b.logdets + 1, info, hlane);
-            if (rc == AJ_OK && with_grad) rc = spd_invert_factor(S, b.wh, info, hlane);
+            rc = spd_factor(b.H, S, b.wh, b.logdets + 1, info, hlane, true, with_grad);
             if (rc == AJ_OK && with_grad) {
                 frob_lower_kernel<<<(unsigned)b.nfrob, 256, 0, hlane>>>(b.wh.Linv, S, b.fpart);
                 rc = check_launch();
@@ -638,7 +637,7 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         AJ_TRY(join_pre());
         add_kernel<<<blocks_for(S * S, 256, 8 * num_sms()), 256, 0, st>>>(b.F, b.H, b.A, S * S);
         AJ_LAUNCHED();
-        AJ_TRY(spd_factor(b.A, S, b.wa, b.logdets + 0, info, st));
+        AJ_TRY(spd_factor(b.A, S, b.wa, b.logdets + 0, info, st, true, with_grad));
         AJ_TRY(spd_solve_vec(S, b.wa, b.D, b.s, info, st));
     } else {
         // the same chain in double-float on the float32 pipe
@@ -698,10 +697,7 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
     if (!with_grad) return AJ_OK;
 
     // adjoint
-    if (!mixed) {
-        AJ_TRY(spd_invert_factor(S, b.wa, info, st));
-        AJ_TRY(spd_inverse_from_factor(S, b.wa, b.Ainv, st));
-    }
+    if (!mixed) AJ_TRY(spd_inverse_from_factor(S, b.wa, b.Ainv, st));
     // dlogE/dlambda (and, mixed, the assembly) on the side lane while st computes the weight
     // gradient; both read only finished data
     if (cudaEventRecord(ln.ev[kEvPre], st) != cudaSuccess || cudaStreamWaitEvent(pre, ln.ev[kEvPre], 0) != cudaSuccess)

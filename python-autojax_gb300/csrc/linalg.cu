@@ -273,8 +273,8 @@ __global__ void logdet_kernel(const double* __restrict__ L, int64_t S, double* _
 
 // --------------------------------------------------- triangular inverse
 
-__global__ void linv_init_kernel(double* __restrict__ Li, int64_t S, const double* __restrict__ dinv) {
-    const int64_t kb = blockIdx.x;
+__global__ void linv_init_kernel(double* __restrict__ Li, int64_t S, const double* __restrict__ dinv, int64_t kb0) {
+    const int64_t kb = kb0 + blockIdx.x;
     const int64_t k0 = kb * NB;
     for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
         const int i = e / NB, j = e % NB;
@@ -423,23 +423,91 @@ SpdWorkspace spd_carve(Carver& cv, int64_t S, bool with_inverse) {
     return w;
 }
 
-int spd_factor(const double* A, int64_t S, SpdWorkspace& w, double* logdet, int* info, cudaStream_t st) {
+int spd_factor(const double* A, int64_t S, SpdWorkspace& w, double* logdet, int* info, cudaStream_t st,
+               bool lookahead, bool with_inverse) {
+    if (with_inverse && !w.Linv) return AJ_ERR_ARG;
     if (S <= 0) return AJ_OK;
     if (A != w.L && cudaMemcpyAsync(w.L, A, sizeof(double) * S * S, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
         return AJ_ERR_CUDA;
     const int64_t nbt = (S + NB - 1) / NB;
-    for (int64_t kb = 0; kb < nbt; ++kb) {
-        const int64_t k0 = kb * NB;
-        chol_diag_kernel<<<1, 256, 0, st>>>(w.L, S, k0, w.dinv + kb * NB * NB, info);
-        AJ_LAUNCHED();
-        const int64_t below = S - k0 - NB;
-        if (below > 0) {
-            chol_panel_kernel<<<(unsigned)((below + 31) / 32), 256, 0, st>>>(w.L, S, k0, w.dinv + kb * NB * NB);
+    if (!lookahead || nbt < 3) {
+        if (with_inverse && cudaMemsetAsync(w.Linv, 0, sizeof(double) * S * S, st) != cudaSuccess) return AJ_ERR_CUDA;
+        for (int64_t kb = 0; kb < nbt; ++kb) {
+            const int64_t k0 = kb * NB;
+            chol_diag_kernel<<<1, 256, 0, st>>>(w.L, S, k0, w.dinv + kb * NB * NB, info);
+            AJ_LAUNCHED();
+            const int64_t below = S - k0 - NB;
+            if (below > 0) {
+                chol_panel_kernel<<<(unsigned)((below + 31) / 32), 256, 0, st>>>(w.L, S, k0, w.dinv + kb * NB * NB);
+                AJ_LAUNCHED();
+                double* P = w.L + (k0 + NB) * S + k0;
+                AJ_TRY(gemm_f64(false, true, below, below, NB, -1.0, P, S, P, S, 1.0, w.L + (k0 + NB) * S + k0 + NB,
+                                S, true, st));
+            }
+        }
+        if (with_inverse) {
+            linv_init_kernel<<<(unsigned)nbt, 256, 0, st>>>(w.Linv, S, w.dinv, 0);
+            AJ_LAUNCHED();
+            for (int64_t kb = 0; kb + 1 < nbt; ++kb) {
+                trtri_step_kernel<<<(unsigned)((nbt - kb - 1) * (kb + 1)), 256, 0, st>>>(w.L, w.Linv, S, kb, w.dinv);
+                AJ_LAUNCHED();
+            }
+        }
+    } else {
+        // One step of lookahead on two lanes (lanes.cu): lane 0 carries the chain (the diagonal
+        // block, the panel below it, and the update of the next block column alone), lane 1 the
+        // rest of each step's trailing update, which then runs beside the next step's chain.  The
+        // next block column also takes the previous step's bulk update, so lane 0 waits for it
+        // before updating that column.
+        // With the inverse, lane 2 runs L^-1's block forward substitution one step behind: its
+        // step kb needs block column kb of L (final after panel kb) and the inverse of diagonal
+        // block kb + 1.
+        Lanes* lp = nullptr;
+        AJ_TRY(lanes_for(st, &lp));
+        Lanes& ln = *lp;
+        const int nl = with_inverse ? 3 : 2;
+        AJ_TRY(lanes_fork(ln, st, nl));
+        cudaStream_t crit = ln.s[0], bulk = ln.s[1], inv = ln.s[2];
+        if (with_inverse && cudaMemsetAsync(w.Linv, 0, sizeof(double) * S * S, inv) != cudaSuccess)
+            return AJ_ERR_CUDA;
+        bool bulk_prev = false;
+        for (int64_t kb = 0; kb < nbt; ++kb) {
+            const int64_t k0 = kb * NB;
+            chol_diag_kernel<<<1, 256, 0, crit>>>(w.L, S, k0, w.dinv + kb * NB * NB, info);
+            AJ_LAUNCHED();
+            if (with_inverse) {
+                AJ_TRY(lane_signal(ln, kEvDiag, 0));
+                AJ_TRY(lane_wait(ln, 2, kEvDiag));
+                linv_init_kernel<<<1, 256, 0, inv>>>(w.Linv, S, w.dinv, kb);
+                AJ_LAUNCHED();
+                if (kb > 0) {
+                    trtri_step_kernel<<<(unsigned)((nbt - kb) * kb), 256, 0, inv>>>(w.L, w.Linv, S, kb - 1, w.dinv);
+                    AJ_LAUNCHED();
+                }
+            }
+            const int64_t below = S - k0 - NB;
+            if (below <= 0) break;
+            chol_panel_kernel<<<(unsigned)((below + 31) / 32), 256, 0, crit>>>(w.L, S, k0, w.dinv + kb * NB * NB);
             AJ_LAUNCHED();
             double* P = w.L + (k0 + NB) * S + k0;
-            AJ_TRY(gemm_f64(false, true, below, below, NB, -1.0, P, S, P, S, 1.0, w.L + (k0 + NB) * S + k0 + NB, S,
-                            true, st));
+            const int64_t cw = below < NB ? below : NB;
+            const int64_t rest = below - cw;
+            if (rest > 0) {
+                AJ_TRY(lane_signal(ln, kEvPanel, 0));
+                AJ_TRY(lane_wait(ln, 1, kEvPanel));
+            }
+            if (bulk_prev) AJ_TRY(lane_wait(ln, 0, kEvUpdate));
+            AJ_TRY(gemm_f64(false, true, below, cw, NB, -1.0, P, S, P, S, 1.0, w.L + (k0 + NB) * S + k0 + NB, S, false,
+                            crit));
+            if (rest > 0) {
+                const int64_t c0 = k0 + NB + cw;
+                AJ_TRY(gemm_f64(false, true, rest, rest, NB, -1.0, P + cw * S, S, P + cw * S, S, 1.0,
+                                w.L + c0 * S + c0, S, true, bulk));
+                AJ_TRY(lane_signal(ln, kEvUpdate, 1));
+            }
+            bulk_prev = rest > 0;
         }
+        AJ_TRY(lanes_join(ln, st, nl));
     }
     dim3 zg(blocks_for(S, 256, 8), (unsigned)(S < 65535 ? S : 65535));
     zero_upper_kernel<<<zg, 256, 0, st>>>(w.L, S);
@@ -457,7 +525,7 @@ int spd_invert_factor(int64_t S, SpdWorkspace& w, int* info, cudaStream_t st) {
     if (!w.Linv) return AJ_ERR_ARG;
     const int64_t nbt = (S + NB - 1) / NB;
     if (cudaMemsetAsync(w.Linv, 0, sizeof(double) * S * S, st) != cudaSuccess) return AJ_ERR_CUDA;
-    linv_init_kernel<<<(unsigned)nbt, 256, 0, st>>>(w.Linv, S, w.dinv);
+    linv_init_kernel<<<(unsigned)nbt, 256, 0, st>>>(w.Linv, S, w.dinv, 0);
     AJ_LAUNCHED();
     for (int64_t kb = 0; kb + 1 < nbt; ++kb) {
         const int64_t tiles = (nbt - kb - 1) * (kb + 1);
@@ -544,8 +612,7 @@ int aj_spd_inverse(const double* A, int64_t S, double* Ainv, double* logdet, voi
     cudaStream_t st = as_stream(stream);
     Carver cv(workspace, workspace_bytes);
     SpdWorkspace w = spd_carve(cv, S, true);
-    AJ_TRY(spd_factor(A, S, w, logdet, info, st));
-    AJ_TRY(spd_invert_factor(S, w, info, st));
+    AJ_TRY(spd_factor(A, S, w, logdet, info, st, true, true));
     return spd_inverse_from_factor(S, w, Ainv, st);
 }
 

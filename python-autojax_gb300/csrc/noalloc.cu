@@ -128,7 +128,8 @@ int aj_spd_solve_noalloc(const double* data_vector, const double* A, int64_t S, 
     // diagonal-block inverses and vectors are produced by the factorisation and solve
     Carver cv(base, noalloc_bytes());
     SpdWorkspace w = spd_carve(cv, S, false);
-    AJ_TRY(spd_factor(A, S, w, nullptr, info, st));
+    // on the caller's stream alone (no side streams are created for it)
+    AJ_TRY(spd_factor(A, S, w, nullptr, info, st, false));
     return spd_solve_vec(S, w, data_vector, out, info, st);
 }
 

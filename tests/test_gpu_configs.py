@@ -193,8 +193,10 @@ def test_mixed_matches_oracle(cfg, lam):
 
     Stated tolerances: logE rel 1e-7 (the target is 1e-6); F 1e-12 of its scale
     (double-float gathers, ~2^-47 a term); s against cond(A) at double-float
-    rounding (2^-47 cond); dlogE/dlambda and the weight gradient as in the
-    small-case mixed tests.
+    rounding (2^-47 cond); the weight gradient as in the small-case mixed
+    tests; dlogE/dlambda as there, or within ten times the movement of the
+    oracle's own value under a double-float-sized perturbation of A, whichever
+    is larger (the backward-error bound of a double-float evaluation).
     """
     import torch
 
@@ -219,8 +221,18 @@ def test_mixed_matches_oracle(cfg, lam):
     cond = ev[-1] / ev[0]
     s_ref = np.linalg.solve(A, ref.data_vector_from(T, d["dirty_image"]))
     assert np.linalg.norm(s - s_ref) / np.linalg.norm(s_ref) <= max(1e-10, 2.0**-47 * cond)
+    # dlogE/dlambda = -1/2 [s^T L s + tr(A^-1 L) - tr(H^-1 L)]: at cond(A) ~1e14 (lambda = 1e-3)
+    # tr(A^-1 L) itself moves when A is perturbed at double-float rounding (2^-47 |A|), so the
+    # bound is also ten times that movement of the oracle's own value
+    L = adjoint.laplacian_from(d["neighbors"], d["neighbors_sizes"])
+    rng = np.random.default_rng(0)
+    E = rng.standard_normal(A.shape) * (2.0**-47 * np.abs(A))
+    Ap = A + 0.5 * (E + E.T)
+    sp = np.linalg.solve(Ap, ref.data_vector_from(T, d["dirty_image"]))
+    moved = abs(-0.5 * (sp @ L @ sp + np.sum(np.linalg.inv(Ap) * L.T) - np.sum(np.linalg.inv(H) * L.T)) - r_dlam)
     trace_scale = d["S"] / lam
-    assert abs(dlam - r_dlam) <= 1e-6 * trace_scale + 1e-5 * abs(r_dlam), (dlam, r_dlam)
+    tol_lam = max(1e-6 * trace_scale + 1e-5 * abs(r_dlam), 10.0 * moved)
+    assert abs(dlam - r_dlam) <= tol_lam, (dlam, r_dlam, tol_lam)
     np.testing.assert_allclose(gw, r_gw, rtol=0, atol=max(1e-5, 2e-15 * cond) * np.abs(r_gw).max())
 
 

@@ -159,10 +159,14 @@ def test_index_out_of_range_raises(aj):
         aj.constant_regularization_matrix_from(1.0, nb, np.array([1, 1], dtype=np.int64))
 
 
-def test_not_positive_definite_raises(aj):
+def test_indefinite_solves_and_singular_raises(aj):
+    """As np.linalg.solve (numba.py:731): an indefinite non-singular A is solved (by the LU
+    fallback), a singular one raises LinAlgError."""
     A = np.array([[1.0, 2.0], [2.0, 1.0]])
+    np.testing.assert_allclose(aj.reconstruction_positive_negative_from(np.ones(2), A),
+                               np.linalg.solve(A, np.ones(2)), rtol=1e-14)
     with pytest.raises(np.linalg.LinAlgError):
-        aj.reconstruction_positive_negative_from(np.ones(2), A)
+        aj.reconstruction_positive_negative_from(np.ones(2), np.array([[1.0, 2.0], [2.0, 4.0]]))
 
 
 def test_empty_visibilities_give_zero_w_tilde(aj):
