@@ -43,8 +43,6 @@ extern "C" {
 #define AJ_INFO_INDEX_RANGE 1       /* an index was outside [0, n) and not -1 */
 #define AJ_INFO_NOT_POSITIVE_DEFINITE 2 /* Cholesky met a pivot <= 0 or NaN */
 #define AJ_INFO_SINGULAR 3              /* LU met an exactly zero (or NaN) pivot */
-#define AJ_INFO_DEVICE_TIMEOUT 4        /* a bounded wait inside a tensor-core kernel expired (a fault of
-                                           the device or the launch, not of the data) */
 
 #define AJ_FP64 0
 #define AJ_MIXED 1

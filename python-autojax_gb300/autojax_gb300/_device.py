@@ -99,8 +99,6 @@ class Call:
             raise np.linalg.LinAlgError(f"{self.name}: matrix is not positive definite (pivot {where})")
         if code == _lib.AJ_INFO_SINGULAR:
             raise np.linalg.LinAlgError(f"{self.name}: Singular matrix (zero pivot {where})")
-        if code == _lib.AJ_INFO_DEVICE_TIMEOUT:
-            raise RuntimeError(f"{self.name}: a tensor-core kernel's bounded wait expired (step {where})")
 
     def out(self, t: torch.Tensor):
         return t.cpu().numpy() if self.numpy_out else t

@@ -22,7 +22,6 @@ AJ_BATCH_BRANCHES = 16
 AJ_INFO_INDEX_RANGE = 1
 AJ_INFO_NOT_POSITIVE_DEFINITE = 2
 AJ_INFO_SINGULAR = 3
-AJ_INFO_DEVICE_TIMEOUT = 4
 AJ_FP64 = 0
 AJ_MIXED = 1
 

@@ -269,8 +269,6 @@ class LogEvidence:
             raise np.linalg.LinAlgError(f"curvature_reg_matrix is not positive definite (pivot {where})")
         if code == _lib.AJ_INFO_INDEX_RANGE:
             raise IndexError(f"index out of range (flat position {where})")
-        if code == _lib.AJ_INFO_DEVICE_TIMEOUT:
-            raise RuntimeError(f"a tensor-core kernel's bounded wait expired (step {where})")
 
 
     # --------------------------------------------------------- host facing
@@ -402,8 +400,6 @@ class LogEvidenceBatch:
                 raise np.linalg.LinAlgError(f"model {i}: curvature_reg_matrix is not positive definite (pivot {where})")
             if code == _lib.AJ_INFO_INDEX_RANGE:
                 raise IndexError(f"model {i}: index out of range (flat position {where})")
-            if code == _lib.AJ_INFO_DEVICE_TIMEOUT:
-                raise RuntimeError(f"model {i}: a tensor-core kernel's bounded wait expired (step {where})")
 
 
 

@@ -87,8 +87,6 @@ struct DfSpd {
     double* vec;     // S scratch
     double* vec2;    // S scratch
     float* part;     // partial sums of the transposed triangular product
-    void* dig;       // one panel's digits for the tensor-core trailing update (df_tc.cu)
-    int* dexp;       // and its rows' scale exponents
 };
 size_t dfspd_bytes(int64_t S, bool with_inverse);
 DfSpd dfspd_carve(Carver& cv, int64_t S, bool with_inverse);
@@ -117,14 +115,6 @@ int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, c
                         cudaStream_t st, const float* AIh = nullptr, const float* AIl = nullptr, bool b_split = false,
                         float* xh = nullptr, float* xl = nullptr);
 int df_frob_lower(const float* h, const float* l, int64_t S, double* partial, int64_t nparts, cudaStream_t st);
-
-// ---- df_tc.cu (the double-float Cholesky's trailing update on the tensor cores)
-
-size_t df_tc_digit_bytes(int64_t S);
-// L (planes, S x S) -= X X^T on the lower triangle of rows and columns r0 .. S-1, X = L[r0:, k0:k0+32];
-// digits (df_tc_digit_bytes(S)) and exps (S ints) are scratch
-int df_tc_update(float* Lh, float* Ll, int64_t S, int64_t k0, int64_t r0, void* digits, int* exps, int* info,
-                 cudaStream_t st);
 
 // ---- wtilde_tc.cu (the mixed direct w_tilde on the tensor cores)
 

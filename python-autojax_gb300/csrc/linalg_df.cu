@@ -1161,8 +1161,6 @@ size_t dfspd_bytes(int64_t S, bool with_inverse) {
     s.take<double>(S);  // vector scratch
     s.take<double>(S);  // vector scratch
     s.take<float>(2 * ((S + TRMV_ROWS - 1) / TRMV_ROWS) * S);  // transposed-product partial sums
-    s.take<char>(df_tc_digit_bytes(S));                         // a panel's digits
-    s.take<int>(S);                                             // their rows' exponents
     return s.total();
 }
 
@@ -1189,8 +1187,6 @@ DfSpd dfspd_carve(Carver& cv, int64_t S, bool with_inverse) {
     w.vec = cv.take<double>(S);
     w.vec2 = cv.take<double>(S);
     w.part = cv.take<float>(2 * ((S + TRMV_ROWS - 1) / TRMV_ROWS) * S);
-    w.dig = cv.take<char>(df_tc_digit_bytes(S));
-    w.dexp = cv.take<int>(S);
     return w;
 }
 
@@ -1386,9 +1382,13 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
         if (tb > 1) {
             AJ_TRY(lane_signal(ln, kEvPanel, 0));
             AJ_TRY(lane_wait(ln, 1, kEvPanel));
-            // the bulk of step kb on the tensor cores (df_tc.cu), every size alike
-            for (int z = 0; z < count; ++z)
-                AJ_TRY(df_tc_update(w[z]->Lh, w[z]->Ll, S, k0, k0 + 2 * DNB, w[z]->dig, w[z]->dexp, info, bulk));
+            const int64_t n64 = (S - k0 - 2 * DNB + T64 - 1) / T64;
+            const int64_t t64 = n64 * (n64 + 1) / 2;
+            if (t64 >= g_tile64_min[0])
+                dfsyrk_update64_kernel<<<dim3((unsigned)t64, count), 256, 0, bulk>>>(m, S, k0);
+            else
+                dfsyrk_update_kernel<<<dim3((unsigned)((tb - 1) * tb / 2), count), 128, 0, bulk>>>(m, S, k0);
+            AJ_LAUNCHED();
             AJ_TRY(lane_signal(ln, kEvUpdate, 1));
         }
         rest_prev = tb > 1;
