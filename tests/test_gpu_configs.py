@@ -259,3 +259,69 @@ def test_compact_table_route_matches_at_size(cfg, precision):
     assert abs(compact - dense) <= tol * abs(dense), (compact, dense)
     exp = ref.log_likelihood_function_via_w_tilde_from(*_args(d, cfg["W"]), coefficient=c)
     assert abs(compact - exp) <= (1e-10 if precision == "fp64" else 1e-7) * abs(exp), (compact, exp)
+
+
+def _cond_at(cfg, coef):
+    d, W, T = cfg["d"], cfg["W"], cfg["T"]
+    H = ref.constant_regularization_matrix_from(coef, d["neighbors"], d["neighbors_sizes"])
+    ev = np.linalg.eigvalsh(ref.curvature_matrix_via_w_tilde_from(W, T) + H)
+    return ev[-1] / ev[0]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_compact_route_gradients_match_dense(cfg, precision):
+    """The gradient from the compact table (W~ never stored: F and Omega = W~ T gathered from the
+    N x (2N - 1) table) against the dense-W~ gradient, at the configuration's sizes."""
+    import torch
+
+    import autojax_gb300 as aj
+
+    d = cfg["d"]
+    dev = cfg["Wd"].device
+    wc = aj.w_compact_curvature_interferometer_from(d["grid_size"], torch.from_numpy(d["noise_map_real"]).to(dev),
+                                                    torch.from_numpy(d["uv_wavelengths"]).to(dev), d["pixel_scale"])
+    nat = torch.from_numpy(d["native_index_for_slim_index"]).to(dev)
+    a = _args(d, cfg["Wd"])
+    dense = aj.log_evidence_and_grad(*a, coefficient=1.0, precision=precision)
+    compact = aj.log_evidence_and_grad(*a[:3], None, *a[4:], coefficient=1.0, precision=precision, w_compact=wc,
+                                       native_index_for_slim_index=nat)
+    cond = _cond_at(cfg, 1.0)
+    tol = 1e-10 if precision == "fp64" else 1e-8
+    assert abs(float(compact[0]) - float(dense[0])) <= tol * abs(float(dense[0]))
+    assert abs(float(compact[1]) - float(dense[1])) <= max(1e-8, 1e-15 * cond) * d["S"] + 1e-6 * abs(float(dense[1]))
+    g_c, g_d = compact[2].cpu().numpy(), dense[2].cpu().numpy()
+    np.testing.assert_allclose(g_c, g_d, rtol=0, atol=max(1e-8, 2e-15 * cond) * np.abs(g_d).max())
+
+
+def test_lens_parameter_gradients_at_size(cfg):
+    """Differentiation at the configuration's sizes: logE and its gradients in the SIS Einstein radius,
+    the S x 2 source-pixel positions and lambda, through the GPU weight builder and adjoint, against
+    the oracle chain (oracle weights, closed-form adjoint, weight VJPs; finite-difference-checked on
+    the small case)."""
+    from test_oracle_weights import oracle_chain
+
+    from autojax_gb300 import lensing, synthetic
+    from autojax_gb300.inversion import Dataset
+    from oracle import mapping_weights as mw
+
+    d = cfg["d"]
+    theta = d["grid_radians_slim"] / synthetic.ARCSEC
+    rng = np.random.default_rng(9)
+    beta0 = mw.sis_trace(theta, 0.8)
+    pts = beta0[rng.choice(beta0.shape[0], d["S"], replace=False)] + 1e-3 * rng.standard_normal((d["S"], 2))
+    simplices, nb, nsz = lensing.triangulate(pts)
+    r = oracle_chain(d, theta, pts, simplices, nb, nsz, cfg["W"], 0.8, 1.0)
+    T = ref.mapping_matrix_from(r[4], mw.delaunay_weights(mw.sis_trace(theta, 0.8), pts, simplices)[1], d["S"])
+    H = ref.constant_regularization_matrix_from(1.0, nb, nsz)
+    ev = np.linalg.eigvalsh(ref.curvature_matrix_via_w_tilde_from(cfg["W"], T) + H)
+    cond = ev[-1] / ev[0]
+    for precision in ("fp64", "mixed"):
+        ds = Dataset(d["dirty_image"], d["data"], d["noise_map"], cfg["Wd"], precision=precision)
+        le = lensing.LensedEvidence(ds, theta, pts)
+        logE, g_te, gP, dlam = le.evaluate(0.8, pts, 1.0)
+        tol = 1e-10 if precision == "fp64" else 1e-8
+        assert abs(logE - r[0]) <= tol * abs(r[0]), (precision, logE, r[0])
+        gtol = max(1e-7 if precision == "fp64" else 1e-5, 2e-15 * cond)
+        assert abs(g_te - r[1]) <= gtol * max(1.0, abs(r[1])), (precision, g_te, r[1])
+        np.testing.assert_allclose(gP, r[2], rtol=0, atol=gtol * np.abs(r[2]).max())
+        assert abs(dlam - r[3]) <= 1e-6 * d["S"] + gtol * abs(r[3]), (precision, dlam, r[3])
