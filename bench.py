@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--skip-wtilde", action="store_true", help="omit the w_tilde kernel measurement")
     ap.add_argument("--stages", action="store_true", help="also time the pipeline stages separately")
     ap.add_argument("--skip-batch", action="store_true", help="omit the batched many-model measurement")
+    ap.add_argument("--skip-roofline", action="store_true", help="omit the standalone roofline group (for ncu)")
     ap.add_argument("--batch", type=int, default=64, help="lens models in the batched measurement")
     ap.add_argument("--only", choices=("roofline", "wtilde"), help="run one kernel measurement alone (for ncu)")
     ap.add_argument("--tile-policy", help="fixed tile policy 'update,inverse,lauum' instead of tuning (for ncu)")
@@ -308,8 +309,11 @@ def roofline(A, dist: Dist, tune_policy: bool = True):
         L, _ = torch.linalg.cholesky_ex(A)
         torch.cholesky_inverse(L)
 
-    inv_vendor(0)
-    t_inv_vendor = time_region(inv_vendor, reps, dist, "roofline_fp64_vendor") / reps
+    try:
+        inv_vendor(0)
+        t_inv_vendor = time_region(inv_vendor, reps, dist, "roofline_fp64_vendor") / reps
+    except RuntimeError:  # torch's linear-algebra library may be unavailable (e.g. under a profiler)
+        t_inv_vendor = None
     fp64_peak = fma_peak_tflops(_lib.AJ_FP64)
     fp32_peak = fma_peak_tflops(_lib.AJ_MIXED)
     df_peak = fp32_peak / 11.4
@@ -331,7 +335,7 @@ def roofline(A, dist: Dist, tune_policy: bool = True):
         "ms": 1e3 * t_inv_mixed,
         "fp64_same_work_ms": 1e3 * t_inv_fp64,
         "fp64_same_work_frac_of_fp64_peak": inv_flops / t_inv_fp64 / 1e12 / fp64_peak,
-        "fp64_vendor_same_work_ms": 1e3 * t_inv_vendor,
+        "fp64_vendor_same_work_ms": 1e3 * t_inv_vendor if t_inv_vendor else None,
         "fp64_vendor_note": "torch.linalg.cholesky_ex + torch.cholesky_inverse in float64 on the same A "
                             "(the vendor solver, not this library): a reference point for the float64 path",
     }
@@ -457,7 +461,10 @@ def gpu_arm(args, dist: Dist) -> dict:
         w_tilde, torch.from_numpy(d["pix_indexes_for_sub_slim_index"]).to(dev),
         torch.from_numpy(d["pix_weights_for_sub_slim_index"]).to(dev), S)
     A = (A + F).contiguous()
-    roof, fp64_peak, fp32_peak = roofline(A, dist, tune_policy=not args.tile_policy)
+    if args.skip_roofline:
+        roof, fp64_peak, fp32_peak = None, fma_peak_tflops(_lib.AJ_FP64), fma_peak_tflops(_lib.AJ_MIXED)
+    else:
+        roof, fp64_peak, fp32_peak = roofline(A, dist, tune_policy=not args.tile_policy)
     del F
 
     result = {
@@ -542,7 +549,16 @@ def batched_bench(args, dev, dist: Dist) -> dict:
     for i, m in enumerate(lm):
         batch.set_model(i, m["pix_indexes_for_sub_slim_index"], m["pix_weights_for_sub_slim_index"], m["neighbors"],
                         m["neighbors_sizes"], m["coefficient"])
+    # the tile policy for throughput: many evaluations in flight favour the bigger tiles that the
+    # latency-bound single evaluation avoids (results do not depend on the policy)
+    from autojax_gb300 import tune
+
+    single_policy = tune.get_tile_policy()
     batch.capture()
+    if args.tile_policy:
+        tuned = {"policy": single_policy, "candidates_timed": 0}
+    else:
+        tuned = tune.tune_tile_policy(batch.step, prepare=batch.capture, reps=2, rounds=1)
     for _ in range(max(2, args.warmup)):
         batch.step()
     torch.cuda.synchronize()
@@ -550,6 +566,8 @@ def batched_bench(args, dev, dist: Dist) -> dict:
     steps = 5
     t = time_region(lambda i: batch.step(), steps, dist, "timed_batch")
     batch.check()
+    # one graph at a time, each captured with the single evaluation's policy
+    tune.set_tile_policy(*single_policy)
     for e in batch.evals:
         e.capture()
     for e in batch.evals:
@@ -570,6 +588,8 @@ def batched_bench(args, dev, dist: Dist) -> dict:
         "batched_over_sequential": t_seq / (t / steps),
         "launches_per_batch": batch.launches_per_batch,
         "graph": True,
+        "tile_policy": {"batch": list(tuned["policy"]), "sequential": list(single_policy),
+                        "candidates_timed": tuned["candidates_timed"]},
     }
 
 

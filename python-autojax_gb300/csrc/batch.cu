@@ -6,17 +6,20 @@
 // are shared and stay resident.  One evaluation is a chain of small,
 // latency-bound launches (the blocked factorisations); run alone it leaves
 // most of the GPU idle.  The batch therefore forks the caller's stream into
-// branch streams, enqueues the evaluations round-robin over the branches, and
+// branch streams, enqueues the evaluations over the branches (balanced, below), and
 // joins them back, so the chains of different evaluations fill each other's
 // gaps.  Captured into one CUDA graph (aj_graph_begin/end), a whole batch is a
-// single graph launch whose branches the GPU runs concurrently.
+// single graph launch whose branches the GPU runs concurrently.  The models go
+// to the branches longest first, each onto the branch with the least work so far.
 //
 // Branch streams are created once per (device, caller stream) on first use,
 // like the factorisation lanes, which are in turn keyed by branch stream, so
 // every evaluation in flight has its own lanes.
 
+#include <algorithm>
 #include <map>
 #include <mutex>
+#include <vector>
 
 #include "aj_internal.cuh"
 
@@ -115,11 +118,29 @@ int aj_log_evidence_batched(const aj_problem* problems, int64_t n, int precision
     if (cudaEventRecord(br->fork, st) != cudaSuccess) return AJ_ERR_CUDA;
     for (int b = 0; b < nb; ++b)
         if (cudaStreamWaitEvent(br->s[b], br->fork, 0) != cudaSuccess) return AJ_ERR_CUDA;
+    // Longest first onto the least-loaded branch: an evaluation's work grows as S^3 (its factorisations)
+    // plus M S (its gathers), and the branches run concurrently, so balancing their loads shortens the
+    // batch.  A model's kernels and their order are the same on any branch, so results do not depend on
+    // the assignment.
+    std::vector<int64_t> order(n);
+    for (int64_t i = 0; i < n; ++i) order[i] = i;
+    auto cost = [&](int64_t i) {
+        const double S = (double)problems[i].S;
+        return S * S * S + 64.0 * (double)problems[i].M * S;
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return cost(a) > cost(b); });
+    std::vector<double> load(nb, 0.0);
     int rc = AJ_OK;
-    for (int64_t i = 0; i < n && rc == AJ_OK; ++i)
+    for (int64_t k = 0; k < n && rc == AJ_OK; ++k) {
+        const int64_t i = order[k];
+        int b = 0;
+        for (int c = 1; c < nb; ++c)
+            if (load[c] < load[b]) b = c;
+        load[b] += cost(i);
         rc = aj_log_evidence(&problems[i], precision, with_grad, out + 2 * i, with_grad ? grad_weights[i] : nullptr,
                              reconstruction ? reconstruction[i] : nullptr, workspaces[i], workspace_bytes[i],
-                             info + 2 * i, br->s[i % nb]);
+                             info + 2 * i, br->s[b]);
+    }
     // join even after a failed enqueue, so the caller's stream never runs ahead of a branch
     for (int b = 0; b < nb; ++b) {
         if (cudaEventRecord(br->join[b], br->s[b]) != cudaSuccess ||
