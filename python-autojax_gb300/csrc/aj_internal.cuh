@@ -32,9 +32,10 @@ size_t spd_workspace_bytes(int64_t S, bool with_inverse);
 SpdWorkspace spd_carve(Carver& cv, int64_t S, bool with_inverse);
 // L = chol(A) (A read, not modified); logdet written to *logdet (device); info on failure.
 // With lookahead the chain and the bulk of each trailing update run on two lanes forked from st;
-// with_inverse also computes Linv = L^-1 (w.Linv), on a third lane one step behind the factor.
+// with_inverse also computes Linv = L^-1 (w.Linv), on a third lane one step behind the factor, and
+// with Ainv (S x S) also A^-1 = L^-T L^-1 (full symmetric), streamed on a fourth lane.
 int spd_factor(const double* A, int64_t S, SpdWorkspace& w, double* logdet, int* info, cudaStream_t st,
-               bool lookahead = true, bool with_inverse = false);
+               bool lookahead = true, bool with_inverse = false, double* Ainv = nullptr);
 // Linv = L^-1 (lower)
 int spd_invert_factor(int64_t S, SpdWorkspace& w, int* info, cudaStream_t st);
 // x = A^-1 b using L (triangular solves); b and x may alias

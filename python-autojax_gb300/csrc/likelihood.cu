@@ -637,7 +637,7 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         AJ_TRY(join_pre());
         add_kernel<<<blocks_for(S * S, 256, 8 * num_sms()), 256, 0, st>>>(b.F, b.H, b.A, S * S);
         AJ_LAUNCHED();
-        AJ_TRY(spd_factor(b.A, S, b.wa, b.logdets + 0, info, st, true, with_grad));
+        AJ_TRY(spd_factor(b.A, S, b.wa, b.logdets + 0, info, st, true, with_grad, with_grad ? b.Ainv : nullptr));
         AJ_TRY(spd_solve_vec(S, b.wa, b.D, b.s, info, st));
     } else {
         // the same chain in double-float on the float32 pipe
@@ -697,7 +697,6 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
     if (!with_grad) return AJ_OK;
 
     // adjoint
-    if (!mixed) AJ_TRY(spd_inverse_from_factor(S, b.wa, b.Ainv, st));
     // dlogE/dlambda (and, mixed, the assembly) on the side lane while st computes the weight
     // gradient; both read only finished data
     if (cudaEventRecord(ln.ev[kEvPre], st) != cudaSuccess || cudaStreamWaitEvent(pre, ln.ev[kEvPre], 0) != cudaSuccess)

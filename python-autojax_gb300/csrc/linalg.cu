@@ -424,8 +424,9 @@ SpdWorkspace spd_carve(Carver& cv, int64_t S, bool with_inverse) {
 }
 
 int spd_factor(const double* A, int64_t S, SpdWorkspace& w, double* logdet, int* info, cudaStream_t st,
-               bool lookahead, bool with_inverse) {
+               bool lookahead, bool with_inverse, double* Ainv) {
     if (with_inverse && !w.Linv) return AJ_ERR_ARG;
+    if (Ainv && !with_inverse) return AJ_ERR_ARG;
     if (S <= 0) return AJ_OK;
     if (A != w.L && cudaMemcpyAsync(w.L, A, sizeof(double) * S * S, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
         return AJ_ERR_CUDA;
@@ -453,6 +454,7 @@ int spd_factor(const double* A, int64_t S, SpdWorkspace& w, double* logdet, int*
                 AJ_LAUNCHED();
             }
         }
+        if (Ainv) AJ_TRY(spd_inverse_from_factor(S, w, Ainv, st));
     } else {
         // One step of lookahead on two lanes (lanes.cu): lane 0 carries the chain (the diagonal
         // block, the panel below it, and the update of the next block column alone), lane 1 the
@@ -462,14 +464,18 @@ int spd_factor(const double* A, int64_t S, SpdWorkspace& w, double* logdet, int*
         // With the inverse, lane 2 runs L^-1's block forward substitution one step behind: its
         // step kb needs block column kb of L (final after panel kb) and the inverse of diagonal
         // block kb + 1.
+        // With A^-1, lane 3 builds it up as L^-T L^-1 one block row of L^-1 at a time: once block row
+        // R is final (after its diagonal block and L^-1's step R - 1), its rank-32 contribution goes
+        // into every lower tile (I, J <= R).
         Lanes* lp = nullptr;
         AJ_TRY(lanes_for(st, &lp));
         Lanes& ln = *lp;
-        const int nl = with_inverse ? 3 : 2;
+        const int nl = Ainv ? 4 : (with_inverse ? 3 : 2);
         AJ_TRY(lanes_fork(ln, st, nl));
-        cudaStream_t crit = ln.s[0], bulk = ln.s[1], inv = ln.s[2];
+        cudaStream_t crit = ln.s[0], bulk = ln.s[1], inv = ln.s[2], lau = ln.s[3];
         if (with_inverse && cudaMemsetAsync(w.Linv, 0, sizeof(double) * S * S, inv) != cudaSuccess)
             return AJ_ERR_CUDA;
+        if (Ainv && cudaMemsetAsync(Ainv, 0, sizeof(double) * S * S, lau) != cudaSuccess) return AJ_ERR_CUDA;
         bool bulk_prev = false;
         for (int64_t kb = 0; kb < nbt; ++kb) {
             const int64_t k0 = kb * NB;
@@ -483,6 +489,15 @@ int spd_factor(const double* A, int64_t S, SpdWorkspace& w, double* logdet, int*
                 if (kb > 0) {
                     trtri_step_kernel<<<(unsigned)((nbt - kb) * kb), 256, 0, inv>>>(w.L, w.Linv, S, kb - 1, w.dinv);
                     AJ_LAUNCHED();
+                }
+                if (Ainv) {
+                    // block row kb of L^-1 is final now
+                    AJ_TRY(lane_signal(ln, kEvRow, 2));
+                    AJ_TRY(lane_wait(ln, 3, kEvRow));
+                    const int64_t m = (kb + 1) * NB < S ? (kb + 1) * NB : S;
+                    const int64_t kr = S - k0 < NB ? S - k0 : NB;
+                    const double* R = w.Linv + k0 * S;
+                    AJ_TRY(gemm_f64(true, false, m, m, kr, 1.0, R, S, R, S, 1.0, Ainv, S, true, lau));
                 }
             }
             const int64_t below = S - k0 - NB;
@@ -508,6 +523,11 @@ int spd_factor(const double* A, int64_t S, SpdWorkspace& w, double* logdet, int*
             bulk_prev = rest > 0;
         }
         AJ_TRY(lanes_join(ln, st, nl));
+        if (Ainv) {
+            dim3 g(blocks_for(S, 256, 8), (unsigned)(S < 65535 ? S : 65535));
+            mirror_lower_kernel<<<g, 256, 0, st>>>(Ainv, S);
+            AJ_LAUNCHED();
+        }
     }
     dim3 zg(blocks_for(S, 256, 8), (unsigned)(S < 65535 ? S : 65535));
     zero_upper_kernel<<<zg, 256, 0, st>>>(w.L, S);
@@ -612,8 +632,7 @@ int aj_spd_inverse(const double* A, int64_t S, double* Ainv, double* logdet, voi
     cudaStream_t st = as_stream(stream);
     Carver cv(workspace, workspace_bytes);
     SpdWorkspace w = spd_carve(cv, S, true);
-    AJ_TRY(spd_factor(A, S, w, logdet, info, st, true, true));
-    return spd_inverse_from_factor(S, w, Ainv, st);
+    return spd_factor(A, S, w, logdet, info, st, true, true, Ainv);
 }
 
 }  // extern "C"
