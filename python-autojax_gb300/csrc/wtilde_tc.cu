@@ -211,17 +211,26 @@ __global__ void __launch_bounds__(kThreads, 1)
                     tc_fence_after();
                     const uint32_t sa = sbase + static_cast<uint32_t>(s * kStageBytes);
                     const uint32_t sb = sa + kStageA;
+                    // A digit d meets B digits e = 0 .. 6 - d back to back, so A stays in the
+                    // collector buffer across them; the d = 0 sweep writes every level first
 #pragma unroll
                     for (int ks = 0; ks < BK / 16; ++ks) {
 #pragma unroll
-                        for (int L = 0; L < kLevels; ++L) {
+                        for (int d = 0; d < kDigits; ++d) {
+                            const uint64_t ad = desc_sw64(sa + d * (BM * BK * 2) + ks * 32);
+                            const uint32_t acc = (sg == 0 && ks == 0 && d == 0) ? 0u : 1u;
 #pragma unroll
-                            for (int d = 0; d <= L; ++d) {
-                                const int e = L - d;
-                                const uint64_t ad = desc_sw64(sa + d * (BM * BK * 2) + ks * 32);
+                            for (int e = 0; e < kDigits - d; ++e) {
                                 const uint64_t bd = desc_sw64(sb + e * (BN * BK * 2) + ks * 32);
-                                const uint32_t acc = (sg == 0 && ks == 0 && d == 0) ? 0u : 1u;
-                                tc_mma(tmem + static_cast<uint32_t>(L * BN), ad, bd, kIdesc, acc);
+                                const uint32_t dst = tmem + static_cast<uint32_t>((d + e) * BN);
+                                if (kDigits - d == 1)
+                                    tc_mma(dst, ad, bd, kIdesc, acc);
+                                else if (e == 0)
+                                    tc_mma_collect<ACollect::kFill>(dst, ad, bd, kIdesc, acc);
+                                else if (e == kDigits - d - 1)
+                                    tc_mma_collect<ACollect::kLastUse>(dst, ad, bd, kIdesc, acc);
+                                else
+                                    tc_mma_collect<ACollect::kUse>(dst, ad, bd, kIdesc, acc);
                             }
                         }
                     }
