@@ -289,7 +289,8 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 // each trailing update runs on another lane.
 constexpr int PANEL_THREADS = 1024;
 constexpr int PANEL_SP = 8;  // sub-panel width of the panel factorisation
-static_assert(PANEL_THREADS >= 3 * 32 && DNB % PANEL_SP == 0, "three chain warps; whole sub-panels");
+static_assert(PANEL_THREADS >= 3 * 32 && PANEL_THREADS % 128 == 0 && DNB % PANEL_SP == 0,
+              "a thread per solved row; whole warps on each sub-partition; whole sub-panels");
 constexpr int PRE_DIGITS = 6;  // 8-bit digits per double-float value in the tensor-core pre-update
 constexpr int PRE_LEVELS = 7;  // digit-product levels i + j kept
 constexpr int PRE_KS = DNB + 8;  // bf16 row stride of the digit planes: conflict-free fragment loads
@@ -454,11 +455,17 @@ __global__ void __launch_bounds__(PANEL_THREADS)
         }
     }
     // Factor the pivot block and solve the panel rows for L's columns, 8 columns (a sub-panel)
-    // at a time.  Warps 0 .. 2 take a sub-panel through in registers, without block barriers:
-    // each holds the sub-panel's 8 x 8 diagonal block in lanes 0 .. 7 (factored identically by
-    // all three) and 32 of the block's rows, which it scales and updates as the columns pass.
-    // Meanwhile the other warps apply the previous sub-panel to the columns past the next
-    // sub-panel; then all warps apply this sub-panel to the next one.
+    // at a time, in three phases a sub-panel:
+    //  A. Warp 0 factors the sub-panel's 8 x 8 diagonal block in lanes 0 .. 7 (one row a lane).
+    //     Meanwhile the warps on the other three SM sub-partitions (warp w runs on sub-partition
+    //     w mod 4) apply the previous sub-panel to the columns past this one.  The pivot chain is
+    //     latency-bound: alone on its sub-partition it takes ~290 cycles a pivot, beside seven
+    //     busy warps ~1,800, so the warps that share warp 0's sub-partition sit this phase out.
+    //  B. One thread a row solves the rows below the diagonal block (the pivot block's and the
+    //     panel's) against it.
+    //  C. All warps apply the sub-panel to the next sub-panel's columns.
+    // Every value is computed by the same operations in the same order as a single chain that
+    // carries all rows through the pivots together, so the factor does not depend on this split.
     const int w = tid >> 5, lane = tid & 31;
     // a[x][c] -= sum_t l[x][p0 + t] l[c][p0 + t] over the block's rows x (the pivot block's only
     // on and below the diagonal) and the columns c0 <= c < c1; work items t0, t0 + nt, ...
@@ -476,58 +483,80 @@ __global__ void __launch_bounds__(PANEL_THREADS)
             pl[x][c] = v.lo;
         }
     };
+    constexpr int kSideWarps = (PANEL_THREADS / 32) * 3 / 4;  // warps off sub-partition 0
     __syncthreads();  // the pre-update's writes
     for (int J = 0; J < DNB / PANEL_SP; ++J) {
         const int j0 = J * PANEL_SP;
-        if (w < 3) {
-            if (w == 0 || rows) {
-                const int x = w * 32 + lane;
-                df y[PANEL_SP], dv[PANEL_SP];
+        if (w == 0) {
+            df dv[PANEL_SP];
 #pragma unroll
-                for (int t = 0; t < PANEL_SP; ++t) {
-                    y[t] = {ph[x][j0 + t], pl[x][j0 + t]};
-                    dv[t] = lane < PANEL_SP ? df{ph[j0 + lane][j0 + t], pl[j0 + lane][j0 + t]} : df{0.f, 0.f};
+            for (int t = 0; t < PANEL_SP; ++t)
+                dv[t] = lane < PANEL_SP ? df{ph[j0 + lane][j0 + t], pl[j0 + lane][j0 + t]} : df{0.f, 0.f};
+            // No branch inside the pivot loop, so the compiler schedules it as one block (the
+            // next pivot's column ahead of this pivot's later ones).  A failed pivot (the same in
+            // every lane) is acted on after the loop; the NaNs it leaves are never stored.  Lane t
+            // keeps pivot t's r = 1 / L_tt for the stores after the loop.
+            int fail = PANEL_SP;
+            df my_r = {0.f, 0.f};
+#pragma unroll
+            for (int t = 0; t < PANEL_SP; ++t) {
+                const df d = {__shfl_sync(0xffffffffu, dv[t].hi, t), __shfl_sync(0xffffffffu, dv[t].lo, t)};
+                fail = (fail == PANEL_SP && !(d.hi > 0.f)) ? t : fail;
+                const df r = dfrsqrt(d);
+                dv[t] = lane == t ? dfmul(d, r) : dfmul(dv[t], r);
+                my_r = lane == t ? r : my_r;
+#pragma unroll
+                for (int u = t + 1; u < PANEL_SP; ++u) {
+                    const df lu = {__shfl_sync(0xffffffffu, dv[t].hi, u), __shfl_sync(0xffffffffu, dv[t].lo, u)};
+                    df_fms_acc(dv[u], dv[t], lu);
                 }
-                bool ok = true;
-#pragma unroll
-                for (int t = 0; t < PANEL_SP; ++t) {
-                    const int j = j0 + t;
-                    const df d = {__shfl_sync(0xffffffffu, dv[t].hi, t), __shfl_sync(0xffffffffu, dv[t].lo, t)};
-                    if (!(d.hi > 0.f)) {  // the same in every lane and every chain warp
-                        if (w == 0 && lane == 0) {
-                            bad = 1;
-                            if (blockIdx.x == 0) report(info, AJ_INFO_NOT_POSITIVE_DEFINITE, k0 + j);
-                        }
-                        ok = false;
-                        break;
-                    }
-                    const df r = dfrsqrt(d);
-                    dv[t] = lane == t ? dfmul(d, r) : dfmul(dv[t], r);
-                    y[t] = x == j ? dfmul(d, r) : dfmul(y[t], r);
-                    if (w == 0 && lane == t) {
-                        rh[j] = r.hi;
-                        rl[j] = r.lo;
-                        if (blockIdx.x == 0 && j < nb) piv[k0 + j] = df_to(dv[t]);
-                    }
-#pragma unroll
-                    for (int u = t + 1; u < PANEL_SP; ++u) {
-                        const df lu = {__shfl_sync(0xffffffffu, dv[t].hi, u), __shfl_sync(0xffffffffu, dv[t].lo, u)};
-                        df_fms_acc(dv[u], dv[t], lu);
-                        df_fms_acc(y[u], y[t], lu);
-                    }
-                }
-                if (ok)
-#pragma unroll
-                    for (int t = 0; t < PANEL_SP; ++t) {
-                        ph[x][j0 + t] = y[t].hi;
-                        pl[x][j0 + t] = y[t].lo;
-                    }
             }
-        } else if (J > 0) {
-            rank_update(j0 - PANEL_SP, j0 + PANEL_SP, DNB, tid - 96, PANEL_THREADS - 96);
+            if (fail < PANEL_SP) {
+                if (lane == 0) {
+                    bad = 1;
+                    if (blockIdx.x == 0) report(info, AJ_INFO_NOT_POSITIVE_DEFINITE, k0 + j0 + fail);
+                }
+            } else if (lane < PANEL_SP) {
+                df l_tt = dv[0];
+#pragma unroll
+                for (int t = 1; t < PANEL_SP; ++t) l_tt = lane == t ? dv[t] : l_tt;
+                rh[j0 + lane] = my_r.hi;
+                rl[j0 + lane] = my_r.lo;
+                if (blockIdx.x == 0 && j0 + lane < nb) piv[k0 + j0 + lane] = df_to(l_tt);
+#pragma unroll
+                for (int t = 0; t < PANEL_SP; ++t) {
+                    ph[j0 + lane][j0 + t] = dv[t].hi;
+                    pl[j0 + lane][j0 + t] = dv[t].lo;
+                }
+            }
+        } else if ((w & 3) != 0 && J > 0) {
+            rank_update(j0 - PANEL_SP, j0 + PANEL_SP, DNB, (w - (w >> 2) - 1) * 32 + lane, kSideWarps * 32);
         }
         __syncthreads();
         if (bad) return;
+        {
+            // rows j0 + 8 .. 31 of the pivot block, then the panel rows
+            const int npiv = DNB - j0 - PANEL_SP;
+            if (tid < npiv + (rows ? 64 : 0)) {
+                const int x = tid < npiv ? j0 + PANEL_SP + tid : DNB + (tid - npiv);
+                df y[PANEL_SP];
+#pragma unroll
+                for (int t = 0; t < PANEL_SP; ++t) y[t] = {ph[x][j0 + t], pl[x][j0 + t]};
+#pragma unroll
+                for (int t = 0; t < PANEL_SP; ++t) {
+                    y[t] = dfmul(y[t], {rh[j0 + t], rl[j0 + t]});
+#pragma unroll
+                    for (int u = t + 1; u < PANEL_SP; ++u)
+                        df_fms_acc(y[u], y[t], {ph[j0 + u][j0 + t], pl[j0 + u][j0 + t]});
+                }
+#pragma unroll
+                for (int t = 0; t < PANEL_SP; ++t) {
+                    ph[x][j0 + t] = y[t].hi;
+                    pl[x][j0 + t] = y[t].lo;
+                }
+            }
+        }
+        __syncthreads();
         if (J + 1 < DNB / PANEL_SP) {
             rank_update(j0, j0 + PANEL_SP, j0 + 2 * PANEL_SP, tid, PANEL_THREADS);
             __syncthreads();
