@@ -88,9 +88,17 @@ struct DfSpd {
     double* vec;     // S scratch
     double* vec2;    // S scratch
     float* part;     // partial sums of the transposed triangular product
+    void* tcws;      // scratch of the tensor-core L^-T L^-1 (with_ainv), or null
+    size_t tcws_bytes;
 };
-size_t dfspd_bytes(int64_t S, bool with_inverse);
-DfSpd dfspd_carve(Carver& cv, int64_t S, bool with_inverse);
+// with_ainv: also the scratch for A^-1 = L^-T L^-1 on the tensor cores (needs with_inverse)
+size_t dfspd_bytes(int64_t S, bool with_inverse, bool with_ainv = false);
+DfSpd dfspd_carve(Carver& cv, int64_t S, bool with_inverse, bool with_ainv = false);
+// A^-1's lower triangle (double-float planes, leading dimension S) = X^T X, X = L^-1 lower, on the
+// tensor cores
+size_t tc_lauum_workspace_bytes(int64_t S);
+int tc_lauum(const float* Xh, const float* Xl, int64_t S, float* Ch, float* Cl, void* ws, size_t bytes,
+             cudaStream_t st);
 int df_split(const double* x, int64_t n, float* hi, float* lo, cudaStream_t st);
 int df_mirror_lower(float* hi, float* lo, int64_t S, cudaStream_t st);
 int df_join(const float* hi, const float* lo, int64_t n, double* x, cudaStream_t st);

@@ -463,8 +463,8 @@ size_t evidence_carve(const aj_problem* p, bool mixed, bool with_grad, void* bas
         b.Ah = cv.take<float>(S * S);
         b.Al = cv.take<float>(S * S);
         {
-            Carver c = sub(dfspd_bytes(S, true));
-            b.da = dfspd_carve(c, S, true);
+            Carver c = sub(dfspd_bytes(S, true, with_grad));
+            b.da = dfspd_carve(c, S, true, with_grad);
         }
         {
             Carver c = sub(dfspd_bytes(S, with_grad));

@@ -1179,9 +1179,10 @@ __global__ void df_frob_lower_kernel(const float* __restrict__ h, const float* _
 
 // ------------------------------------------------------------ host side
 
-size_t dfspd_bytes(int64_t S, bool with_inverse) {
+size_t dfspd_bytes(int64_t S, bool with_inverse, bool with_ainv) {
     const int64_t nbt = (S + DNB - 1) / DNB;
     Sizer s;
+    if (with_inverse && with_ainv) s.take<char>(tc_lauum_workspace_bytes(S));
     s.take<float>(2 * S * S);  // L planes
     if (with_inverse) s.take<float>(2 * S * S);
     s.take<float>(2 * nbt * DNB * DNB);  // diagonal-block inverses
@@ -1193,9 +1194,16 @@ size_t dfspd_bytes(int64_t S, bool with_inverse) {
     return s.total();
 }
 
-DfSpd dfspd_carve(Carver& cv, int64_t S, bool with_inverse) {
+DfSpd dfspd_carve(Carver& cv, int64_t S, bool with_inverse, bool with_ainv) {
     const int64_t nbt = (S + DNB - 1) / DNB;
     DfSpd w;
+    if (with_inverse && with_ainv) {
+        w.tcws_bytes = tc_lauum_workspace_bytes(S);
+        w.tcws = cv.take<char>(w.tcws_bytes);
+    } else {
+        w.tcws = nullptr;
+        w.tcws_bytes = 0;
+    }
     float* L = cv.take<float>(2 * S * S);
     w.Lh = L;
     w.Ll = L ? L + S * S : nullptr;
@@ -1352,7 +1360,12 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
     Lanes* lanes = nullptr;
     AJ_TRY(lanes_for(st, &lanes));
     Lanes& ln = *lanes;
-    const int nlanes = AIh ? 5 : 2 + n_inverse;  // lanes 2 .. 1 + n_inverse for L^-1, lane 4 for A^-1
+    // A^-1 = L^-T L^-1: on the tensor cores after the factorisation when matrix 0 has the scratch
+    // for it, otherwise streamed in double-float on lane 4, one finished block row of L^-1 at a time
+    // (the tensor-core product streamed by 256-row slabs on lane 4 measured slower in the batch,
+    // 572 against 596 evaluations/s, and no faster alone: its CTAs, one an SM, crowd the panels)
+    const bool tc_ainv = AIh && w[0]->tcws;
+    const int nlanes = (AIh && !tc_ainv) ? 5 : 2 + n_inverse;  // lanes 2 .. 1 + n_inverse: L^-1; 4: A^-1
     AJ_TRY(lanes_fork(ln, st, nlanes));
     cudaStream_t crit = ln.s[0], bulk = ln.s[1];
     // each matrix's L^-1 on its own lane: a view of m whose slot 0 is matrix z
@@ -1401,7 +1414,7 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
     // that column); the bulk update of step kb covers the columns after it.
     cudaStream_t lau = ln.s[4];
     AJ_TRY(panel(0));
-    if (AIh && nbt == 1) AJ_TRY(lauum_row(0, crit));
+    if (AIh && !tc_ainv && nbt == 1) AJ_TRY(lauum_row(0, crit));
     bool rest_prev = false;
     for (int64_t kb = 0; kb + 1 < nbt; ++kb) {
         const int64_t k0 = kb * DNB;
@@ -1439,7 +1452,7 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
                 }
             }
             // block row 0 of L^-1 is final since panel 0, block row kb + 1 after this step
-            if (AIh) {
+            if (AIh && !tc_ainv) {
                 AJ_TRY(lane_signal(ln, kEvRow, 2));
                 AJ_TRY(lane_wait(ln, 4, kEvRow));
                 if (kb == 0) AJ_TRY(lauum_row(0, lau));
@@ -1459,6 +1472,7 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
         AJ_LAUNCHED();
     }
     AJ_TRY(lanes_join(ln, st, nlanes));
+    if (tc_ainv) AJ_TRY(tc_lauum(w[0]->Ih, w[0]->Il, S, AIh, AIl, w[0]->tcws, w[0]->tcws_bytes, st));
     return AIh ? df_mirror_lower(AIh, AIl, S, st) : AJ_OK;
 }
 
@@ -1536,7 +1550,7 @@ size_t aj_spd_inverse_mixed_workspace_size(int64_t S) {
     Sizer s;
     s.take<float>(2 * S * S);  // A planes
     s.take<float>(2 * S * S);  // A^-1 planes
-    s.take<char>(dfspd_bytes(S, true));
+    s.take<char>(dfspd_bytes(S, true, true));
     return s.total();
 }
 
@@ -1550,9 +1564,9 @@ int aj_spd_inverse_mixed(const double* A, int64_t S, double* Ainv, double* logde
     Carver cv(workspace, workspace_bytes);
     float* Ap = cv.take<float>(2 * S * S);
     float* Ip = cv.take<float>(2 * S * S);
-    char* sub = cv.take<char>(dfspd_bytes(S, true));
-    Carver sc(sub, dfspd_bytes(S, true));
-    DfSpd w = dfspd_carve(sc, S, true);
+    char* sub = cv.take<char>(dfspd_bytes(S, true, true));
+    Carver sc(sub, dfspd_bytes(S, true, true));
+    DfSpd w = dfspd_carve(sc, S, true, true);
     AJ_TRY(df_split(A, S * S, Ap, Ap + S * S, st));
     const float* ah[1] = {Ap};
     const float* al[1] = {Ap + S * S};

@@ -34,34 +34,42 @@
 #include <cuda_bf16.h>
 #include <math.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "aj_internal.cuh"
+#include "df32.cuh"
 #include "tc_common.cuh"
 
 namespace aj {
 
 namespace tc {
 
-constexpr int kDigits = 7;
+constexpr int kDigits = 7;                  // digits a value in the w_tilde product
+constexpr int kInvDigits = 8;               // digits a value in L^-T L^-1 (below)
 constexpr int kDigitBits = 7;
 constexpr int kFirstBits = 6;  // y in [-1, 1]: the first digit rint(y 2^6) lies in [-64, 64]
-constexpr int kLevels = kDigits;            // levels 0 .. kDigits - 1
 constexpr int BM = 128, BN = 64, BK = 32;   // tile rows, tile columns, k rows a stage
 constexpr int kGroupRows = 256;             // rows summed in TMEM between epilogue folds
 constexpr int kStagesPerGroup = kGroupRows / BK;
-constexpr int kStageA = kDigits * BM * BK * 2;  // bytes
-constexpr int kStageB = kDigits * BN * BK * 2;
-constexpr int kStageBytes = kStageA + kStageB;
 constexpr int kStages = 2;
-constexpr int kTmemCols = 512;              // >= kLevels * BN, a power of two
+constexpr int kTmemCols = 512;              // >= levels * BN, a power of two
 constexpr int kThreads = 192;
-constexpr size_t kSmemBytes = size_t(kStages) * kStageBytes + 1024 + 256;
 
-static_assert(kLevels * BN <= kTmemCols, "level accumulators exceed TMEM");
-static_assert((kLevels) * kGroupRows * (1 << (2 * (kDigitBits - 1))) < (1 << 23), "level sums must stay exact");
+// Sizes for ND digits a value: ND levels 0 .. ND - 1, each an N = 64 TMEM accumulator.  Level L
+// sums L + 1 <= ND digit pairs, so a level sum over a group stays within ND kGroupRows 2^12 <= 2^23,
+// an integer float32 holds exactly.
+template <int ND>
+struct Cut {
+    static constexpr int kStageA = ND * BM * BK * 2;  // bytes
+    static constexpr int kStageB = ND * BN * BK * 2;
+    static constexpr int kStageBytes = kStageA + kStageB;
+    static constexpr size_t kSmemBytes = size_t(kStages) * kStageBytes + 1024 + 256;
+    static_assert(ND * BN <= kTmemCols, "level accumulators exceed TMEM");
+    static_assert(ND * kGroupRows * (1 << (2 * (kDigitBits - 1))) <= (1 << 23), "level sums must stay exact");
+    static_assert(kSmemBytes <= 232448, "shared memory");
+};
 static_assert(kGroupRows % BK == 0, "group of whole stages");
-static_assert(kSmemBytes <= 232448, "shared memory");
 
 struct Shared {
     uint64_t full[kStages];
@@ -111,16 +119,29 @@ __device__ __forceinline__ void two_sum_into(float& hi, float& lo, float c) {
     lo += e;
 }
 
-// Out (+)= s2 * acc on the lower triangle of one 128 x 64 tile, as double-float planes.
+// x 2^k, exact while the result stays in the normal range (two power-of-two factors, each a float)
+__device__ __forceinline__ float times_pow2(float x, int k) {
+    k = max(-252, min(252, k));
+    const int k1 = k / 2;
+    return x * __int_as_float((k1 + 127) << 23) * __int_as_float((k - k1 + 127) << 23);
+}
+
+// Out (+)= scale 2^(e_i + e_j) acc on the lower triangle of one 128 x 64 tile (e = 0 without exps).
 __device__ __forceinline__ void store_row(float* __restrict__ oh, float* __restrict__ ol, int64_t ld, int64_t M,
                                           int64_t gi, int64_t gj0, const float (&h)[BN], const float (&l)[BN],
-                                          float scale, int accumulate) {
+                                          float scale, const int* __restrict__ exps, int accumulate) {
     if (gi >= M) return;
+    const int ei = exps ? exps[gi] : 0;
 #pragma unroll
     for (int j = 0; j < BN; ++j) {
         const int64_t gj = gj0 + j;
         if (gj > gi || gj >= M) continue;
         float ah = h[j] * scale, al = l[j] * scale;
+        if (exps) {
+            const int k = ei + exps[gj];
+            ah = times_pow2(ah, k);
+            al = times_pow2(al, k);
+        }
         if (accumulate) {
             const float bh = oh[gi * ld + gj], bl = ol[gi * ld + gj];
             const float s = ah + bh;
@@ -139,20 +160,26 @@ __device__ __forceinline__ void store_row(float* __restrict__ oh, float* __restr
     }
 }
 
-// One CTA per lower tile; Rc rows of digits (a multiple of kGroupRows).  s2 = s^2 2^-(2 first bits).
+// One CTA per lower tile; Rc rows of digits (a multiple of kGroupRows).  The product is scaled by
+// *scale_dev (s^2 2^-(2 first bits)) and, with exps, by 2^(e_i + e_j) per entry (digits of column
+// i cut at its own power of two).  With tri, a digit row k is zero for k < i (the panel is an upper
+// triangle, as the transpose of L^-1 is): a tile starts at the group holding its first row.
+template <int ND>
 __global__ void __launch_bounds__(kThreads, 1)
     digit_syrk_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                       int64_t Rc, int64_t M, int64_t Mp, float* __restrict__ out_h, float* __restrict__ out_l,
-                      int64_t ld,
-                      const float* __restrict__ scale_dev, int accumulate, int* __restrict__ err) {
+                      int64_t ld, const float* __restrict__ scale_dev, const int* __restrict__ exps, int tri,
+                      int accumulate, int* __restrict__ err) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    Shared* sh = reinterpret_cast<Shared*>(base + size_t(kStages) * kStageBytes);
+    Shared* sh = reinterpret_cast<Shared*>(base + size_t(kStages) * Cut<ND>::kStageBytes);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int64_t I, J;
     tile_of(blockIdx.x, Mp / BM, I, J);
-    const int ngroups = static_cast<int>(Rc / kGroupRows);
+    const int g0 = tri ? static_cast<int>(max(I * BM, J * BN) / kGroupRows) : 0;
+    const int ngroups = static_cast<int>(Rc / kGroupRows) - g0;  // groups this tile sums, from g0
     const int nstages = ngroups * kStagesPerGroup;
+    const int it0 = g0 * kStagesPerGroup;  // the first stage's k slab
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
@@ -179,10 +206,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int it = 0; it < nstages; ++it) {
                 const int s = it % kStages;
                 if (it >= kStages && !mbar_wait(&sh->empty[s], ((it / kStages) & 1) ^ 1, abort, err)) break;
-                unsigned char* sa = base + size_t(s) * kStageBytes;
-                mbar_expect_tx(&sh->full[s], kStageBytes);
-                tma_load_3d(sa, &map_a, it * BK, static_cast<int>(I * BM), 0, &sh->full[s]);
-                tma_load_3d(sa + kStageA, &map_b, it * BK, static_cast<int>(J * BN), 0, &sh->full[s]);
+                unsigned char* sa = base + size_t(s) * Cut<ND>::kStageBytes;
+                mbar_expect_tx(&sh->full[s], Cut<ND>::kStageBytes);
+                tma_load_3d(sa, &map_a, (it0 + it) * BK, static_cast<int>(I * BM), 0, &sh->full[s]);
+                tma_load_3d(sa + Cut<ND>::kStageA, &map_b, (it0 + it) * BK, static_cast<int>(J * BN), 0, &sh->full[s]);
                 ++issued;
             }
             // drain: every issued load lands before the CTA may leave (a no-op on the normal path,
@@ -209,25 +236,25 @@ __global__ void __launch_bounds__(kThreads, 1)
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t sa = sbase + static_cast<uint32_t>(s * kStageBytes);
-                    const uint32_t sb = sa + kStageA;
+                    const uint32_t sa = sbase + static_cast<uint32_t>(s * Cut<ND>::kStageBytes);
+                    const uint32_t sb = sa + Cut<ND>::kStageA;
                     // A digit d meets B digits e = 0 .. 6 - d back to back, so A stays in the
                     // collector buffer across them; the d = 0 sweep writes every level first
 #pragma unroll
                     for (int ks = 0; ks < BK / 16; ++ks) {
 #pragma unroll
-                        for (int d = 0; d < kDigits; ++d) {
+                        for (int d = 0; d < ND; ++d) {
                             const uint64_t ad = desc_sw64(sa + d * (BM * BK * 2) + ks * 32);
                             const uint32_t acc = (sg == 0 && ks == 0 && d == 0) ? 0u : 1u;
 #pragma unroll
-                            for (int e = 0; e < kDigits - d; ++e) {
+                            for (int e = 0; e < ND - d; ++e) {
                                 const uint64_t bd = desc_sw64(sb + e * (BN * BK * 2) + ks * 32);
                                 const uint32_t dst = tmem + static_cast<uint32_t>((d + e) * BN);
-                                if (kDigits - d == 1)
+                                if (ND - d == 1)
                                     tc_mma(dst, ad, bd, kIdesc, acc);
                                 else if (e == 0)
                                     tc_mma_collect<ACollect::kFill>(dst, ad, bd, kIdesc, acc);
-                                else if (e == kDigits - d - 1)
+                                else if (e == ND - d - 1)
                                     tc_mma_collect<ACollect::kLastUse>(dst, ad, bd, kIdesc, acc);
                                 else
                                     tc_mma_collect<ACollect::kUse>(dst, ad, bd, kIdesc, acc);
@@ -259,7 +286,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (!mbar_wait(&sh->accfull, g & 1, abort, err)) break;
             tc_fence_after();
 #pragma unroll 1
-            for (int L = kLevels - 1; L >= 0; --L) {
+            for (int L = ND - 1; L >= 0; --L) {
                 const float sc = ldexpf(1.0f, -kDigitBits * L);
 #pragma unroll
                 for (int half = 0; half < BN / 32; ++half) {
@@ -281,7 +308,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         if (!*abort) {
             const int64_t gi = I * BM + q * 32 + lane;
-            store_row(out_h, out_l, ld, M, gi, J * BN, h, l, *scale_dev, accumulate);
+            store_row(out_h, out_l, ld, M, gi, J * BN, h, l, *scale_dev, exps, accumulate);
         }
     }
     tc_fence_before();
@@ -382,13 +409,13 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// the [kDigits][Mp][Rc] bf16 panel seen as boxes of {BK k, rows, kDigits}
-int make_map(CUtensorMap* map, const void* D, int64_t Rc, int64_t Mp, int rows) {
+// the [nd][Mp][Rc] bf16 panel seen as boxes of {BK k, rows, nd}
+int make_map(CUtensorMap* map, const void* D, int64_t Rc, int64_t Mp, int rows, int nd) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return AJ_ERR_CUDA;
-    const cuuint64_t dims[3] = {static_cast<cuuint64_t>(Rc), static_cast<cuuint64_t>(Mp), kDigits};
+    const cuuint64_t dims[3] = {static_cast<cuuint64_t>(Rc), static_cast<cuuint64_t>(Mp), static_cast<cuuint64_t>(nd)};
     const cuuint64_t strides[2] = {static_cast<cuuint64_t>(Rc) * 2, static_cast<cuuint64_t>(Mp * Rc) * 2};
-    const cuuint32_t box[3] = {BK, static_cast<cuuint32_t>(rows), kDigits};
+    const cuuint32_t box[3] = {BK, static_cast<cuuint32_t>(rows), static_cast<cuuint32_t>(nd)};
     const cuuint32_t estr[3] = {1, 1, 1};
     const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(D), dims, strides, box, estr,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -396,6 +423,7 @@ int make_map(CUtensorMap* map, const void* D, int64_t Rc, int64_t Mp, int rows) 
     return r == CUDA_SUCCESS ? AJ_OK : AJ_ERR_CUDA;
 }
 
+template <int ND>
 int set_smem_attr() {
     static std::mutex mu;
     static bool done[64] = {};
@@ -403,25 +431,28 @@ int set_smem_attr() {
     if (cudaGetDevice(&dev) != cudaSuccess) return AJ_ERR_CUDA;
     std::lock_guard<std::mutex> lock(mu);
     if (dev >= 0 && dev < 64 && done[dev]) return AJ_OK;
-    if (cudaFuncSetAttribute(digit_syrk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(kSmemBytes)) != cudaSuccess)
+    if (cudaFuncSetAttribute(digit_syrk_kernel<ND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(Cut<ND>::kSmemBytes)) != cudaSuccess)
         return AJ_ERR_CUDA;
     if (dev >= 0 && dev < 64) done[dev] = true;
     return AJ_OK;
 }
 
+// The lower block triangle of sum_L 2^-7L sum_{d+e=L} D_d D_e^T over the panel's Rc rows, for ND
+// (kDigits or kInvDigits) digit planes.
+template <int ND>
 int launch_syrk(const void* D, int64_t Rc, int64_t M, int64_t Mp, float* oh, float* ol, int64_t ld,
-                const float* scale_dev, int accumulate, int* err, cudaStream_t st) {
+                const float* scale_dev, const int* exps, int tri, int accumulate, int* err, cudaStream_t st) {
     if (Rc <= 0 || Rc % kGroupRows != 0 || Mp % BM != 0 || Mp < M) return AJ_ERR_ARG;
     if (reinterpret_cast<uintptr_t>(D) % 16 != 0) return AJ_ERR_ARG;
     CUtensorMap ma, mb;
-    AJ_TRY(make_map(&ma, D, Rc, Mp, BM));
-    AJ_TRY(make_map(&mb, D, Rc, Mp, BN));
-    AJ_TRY(set_smem_attr());
+    AJ_TRY(make_map(&ma, D, Rc, Mp, BM, ND));
+    AJ_TRY(make_map(&mb, D, Rc, Mp, BN, ND));
+    AJ_TRY(set_smem_attr<ND>());
     const int64_t nI = Mp / BM;
     const int64_t tiles = nI * (nI + 1);
-    digit_syrk_kernel<<<static_cast<unsigned>(tiles), kThreads, kSmemBytes, st>>>(ma, mb, Rc, M, Mp, oh, ol, ld,
-                                                                                 scale_dev, accumulate, err);
+    digit_syrk_kernel<ND><<<static_cast<unsigned>(tiles), kThreads, Cut<ND>::kSmemBytes, st>>>(
+        ma, mb, Rc, M, Mp, oh, ol, ld, scale_dev, exps, tri, accumulate, err);
     return check_launch();
 }
 
@@ -484,9 +515,130 @@ int wtilde_tc(const double* sigma, const double* uv, const double* grid, int64_t
         dim3 g(static_cast<unsigned>((p.kc + 255) / 256), static_cast<unsigned>(p.Mp < 65535 ? p.Mp : 65535));
         tc::wtilde_digits_kernel<<<g, 256, 0, st>>>(sigma, uv, grid, K, M, ch * p.kc, p.kc, p.Mp, ints, D);
         AJ_LAUNCHED();
-        AJ_TRY(tc::launch_syrk(D, p.Rc, M, p.Mp, ph, pl, M, scale, ch > 0 ? 1 : 0, ints + 1, st));
+        AJ_TRY(tc::launch_syrk<tc::kDigits>(D, p.Rc, M, p.Mp, ph, pl, M, scale, nullptr, 0, ch > 0 ? 1 : 0, ints + 1, st));
     }
     tc::poison_on_error_kernel<<<1, 1, 0, st>>>(ints + 1, ph);
+    return check_launch();
+}
+
+// ------------------------------------------- A^-1 = L^-T L^-1 on the tensor cores
+//
+// With X = L^-1 (lower, double-float planes), A^-1[i][j] = sum_k X[k][i] X[k][j]: the product
+// above with "pixels" the columns of X and the reduction over its rows.  Column i is cut into
+// kInvDigits = 8 digits (55 bits) at its own power of two 2^e_i > max_k |X[k][i]|; a column of X
+// has 2-norm sqrt(A^-1_ii), so an entry's truncation error stays below the double-float rounding
+// of sum_k |X[k][i] X[k][j]|.  Rows k < i of X are zero, so a tile starts at the group holding its
+// first row.
+
+namespace tc {
+
+struct LauumPlan {
+    int64_t Sp, Rc;
+};
+
+LauumPlan lauum_plan(int64_t S) {
+    LauumPlan p;
+    p.Sp = (S + BM - 1) / BM * BM;
+    p.Rc = (S + kGroupRows - 1) / kGroupRows * kGroupRows;  // >= Sp: every tile has a group to sum
+    return p;
+}
+
+// colmax[i] = the bits of max_k |Xh[k][i]| (non-negative floats order as their bits)
+__global__ void col_absmax_kernel(const float* __restrict__ Xh, int64_t S, unsigned* __restrict__ colmax) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= S) return;
+    unsigned m = 0;
+    for (int64_t k = blockIdx.y; k < S; k += gridDim.y) m = max(m, __float_as_uint(fabsf(Xh[k * S + i])));
+    atomicMax(&colmax[i], m);
+}
+
+// 2^e > |x| for every x of a column whose largest |hi| has the bits m (0 for a zero column)
+__device__ __forceinline__ int col_exp(unsigned m) {
+    if (m == 0u) return 0;
+    const int be = static_cast<int>((m >> 23) & 0xffu);
+    return be > 0 ? be - 126 : -126;
+}
+
+// D[d][i][k] = digit d of X[k][i] 2^(kFirstBits - e_i) for k < Rc, i < Sp (zero outside S x S),
+// through a 32 x 32 shared-memory transpose; blocks (0, y) also write e_i, block (0, 0) the scale.
+__global__ void __launch_bounds__(256)
+    lauum_digits_kernel(const float* __restrict__ Xh, const float* __restrict__ Xl, int64_t S, int64_t Sp, int64_t Rc,
+                        const unsigned* __restrict__ colmax, int* __restrict__ exps, float* __restrict__ scale,
+                        __nv_bfloat16* __restrict__ D) {
+    __shared__ float th[32][33], tl[32][33];
+    const int64_t k0 = blockIdx.x * 32ll, i0 = blockIdx.y * 32ll;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int64_t k = k0 + ty + 8 * r, i = i0 + tx;
+        const bool in = k < S && i < S;
+        th[ty + 8 * r][tx] = in ? Xh[k * S + i] : 0.f;
+        tl[ty + 8 * r][tx] = in ? Xl[k * S + i] : 0.f;
+    }
+    if (blockIdx.x == 0 && ty == 0) {
+        const int64_t i = i0 + tx;
+        exps[i] = i < S ? col_exp(colmax[i]) : 0;
+        if (blockIdx.y == 0 && tx == 0) *scale = ldexpf(1.0f, -2 * kFirstBits);
+    }
+    __syncthreads();
+    const int64_t plane = Sp * Rc;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int il = ty + 8 * r;
+        const int64_t i = i0 + il, k = k0 + tx;
+        const int e = i < S ? col_exp(colmax[i]) : 0;
+        // y = x 2^(kFirstBits - e), |y| < 2^kFirstBits; each digit leaves an exact remainder
+        float yh = times_pow2(th[tx][il], kFirstBits - e), yl = times_pow2(tl[tx][il], kFirstBits - e);
+        __nv_bfloat16* dst = D + i * Rc + k;
+#pragma unroll
+        for (int d = 0; d < kInvDigits; ++d) {
+            const float q = rintf(yh);
+            dst[d * plane] = __float2bfloat16_rn(q);
+            float sh, se;
+            two_sum(yh - q, yl, sh, se);
+            yh = sh * static_cast<float>(1 << kDigitBits);
+            yl = se * static_cast<float>(1 << kDigitBits);
+        }
+    }
+}
+
+}  // namespace tc
+
+size_t tc_lauum_workspace_bytes(int64_t S) {
+    const tc::LauumPlan p = tc::lauum_plan(S);
+    Sizer s;
+    s.take<__nv_bfloat16>(size_t(tc::kInvDigits) * p.Sp * p.Rc);
+    s.take<unsigned>(p.Sp);
+    s.take<int>(p.Sp);
+    s.take<int>(1);
+    s.take<float>(1);
+    return s.total();
+}
+
+// C's lower triangle (double-float planes, leading dimension S) = X^T X for the lower-triangular
+// X; the upper triangle is left alone.  An expired wait inside the product leaves NaN in C[0][0].
+int tc_lauum(const float* Xh, const float* Xl, int64_t S, float* Ch, float* Cl, void* ws, size_t bytes,
+             cudaStream_t st) {
+    if (S <= 0) return AJ_OK;
+    if (bytes < tc_lauum_workspace_bytes(S)) return AJ_ERR_WORKSPACE;
+    const tc::LauumPlan p = tc::lauum_plan(S);
+    Carver cv(ws, bytes);
+    auto* D = cv.take<__nv_bfloat16>(size_t(tc::kInvDigits) * p.Sp * p.Rc);
+    unsigned* colmax = cv.take<unsigned>(p.Sp);
+    int* exps = cv.take<int>(p.Sp);
+    int* err = cv.take<int>(1);
+    float* scale = cv.take<float>(1);
+    if (cudaMemsetAsync(colmax, 0, sizeof(unsigned) * p.Sp, st) != cudaSuccess ||
+        cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess)
+        return AJ_ERR_CUDA;
+    const unsigned rows_split = static_cast<unsigned>(S < 64 ? S : 64);
+    tc::col_absmax_kernel<<<dim3(static_cast<unsigned>((S + 255) / 256), rows_split), 256, 0, st>>>(Xh, S, colmax);
+    AJ_LAUNCHED();
+    tc::lauum_digits_kernel<<<dim3(static_cast<unsigned>(p.Rc / 32), static_cast<unsigned>(p.Sp / 32)), 256, 0, st>>>(
+        Xh, Xl, S, p.Sp, p.Rc, colmax, exps, scale, D);
+    AJ_LAUNCHED();
+    AJ_TRY(tc::launch_syrk<tc::kInvDigits>(D, p.Rc, S, p.Sp, Ch, Cl, S, scale, exps, 1, 0, err, st));
+    tc::poison_on_error_kernel<<<1, 1, 0, st>>>(err, Ch);
     return check_launch();
 }
 
@@ -500,7 +652,8 @@ int aj_digit_syrk_probe(const void* digits, int64_t rows, int64_t M, float* out_
                         const float* scale, int accumulate, int* err, void* stream) {
     if (!digits || !out_hi || !out_lo || !scale || !err || M <= 0 || rows <= 0) return AJ_ERR_ARG;
     const int64_t Mp = (M + tc::BM - 1) / tc::BM * tc::BM;
-    return tc::launch_syrk(digits, rows, M, Mp, out_hi, out_lo, M, scale, accumulate, err, as_stream(stream));
+    return tc::launch_syrk<tc::kDigits>(digits, rows, M, Mp, out_hi, out_lo, M, scale, nullptr, 0, accumulate, err,
+                           as_stream(stream));
 }
 
 }  // extern "C"

@@ -176,6 +176,40 @@ def test_mixed_spd_inverse_matches_numpy(S):
     assert abs(float(logdet[0]) - ld) <= max(S, 32) * 2.0**-47 * cond * max(1.0, abs(ld))
 
 
+@pytest.mark.parametrize("S", [130, 600, 1500])
+def test_mixed_spd_inverse_with_graded_scales(S):
+    """A = D B D with D = diag(2^u), u in [-20, 20]: the columns of L^-1 span 2^80, so the tensor-core
+    L^-T L^-1 (digits cut per column at its own power of two, groups above a tile's first row
+    skipped) must keep each entry to its own scale, |err_ij| <= tol sqrt(A^-1_ii A^-1_jj), with
+    tol ~ S 2^-46 cond(B) (the double-float bound of the factorisation and inverse)."""
+    import torch
+
+    from autojax_gb300 import _lib
+
+    lib = _lib.load()
+    rng = np.random.default_rng(S)
+    cond = 1e3
+    Bm = _spd_with_condition(S, cond, 100 + S)
+    d = 2.0 ** rng.integers(-20, 21, size=S).astype(np.float64)
+    A = (d[:, None] * Bm) * d[None, :]
+    At = torch.from_numpy(A).cuda()
+    inv = torch.empty_like(At)
+    logdet = torch.zeros(1, dtype=torch.float64, device="cuda")
+    info = torch.zeros(2, dtype=torch.int32, device="cuda")
+    ws = torch.empty(lib.aj_spd_inverse_mixed_workspace_size(S), dtype=torch.uint8, device="cuda")
+    _lib.check(lib.aj_spd_inverse_mixed(At.data_ptr(), S, inv.data_ptr(), logdet.data_ptr(), ws.data_ptr(),
+                                        ws.numel(), info.data_ptr(), torch.cuda.current_stream().cuda_stream),
+               "aj_spd_inverse_mixed")
+    torch.cuda.synchronize()
+    assert int(info[0]) == 0
+    ref = (np.linalg.inv(Bm) / d[:, None]) / d[None, :]
+    got = inv.cpu().numpy()
+    scale = np.sqrt(np.outer(np.diag(ref), np.diag(ref)))
+    tol = S * 2.0**-46 * cond
+    assert np.max(np.abs(got - ref) / scale) <= tol
+    assert np.abs(got - got.T).max() == 0.0
+
+
 def test_mixed_spd_inverse_reports_not_positive_definite():
     import torch
 
