@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--skip-roofline", action="store_true", help="omit the standalone roofline group (for ncu)")
     ap.add_argument("--batch", type=int, default=64, help="lens models in the batched measurement")
     ap.add_argument("--only", choices=("roofline", "wtilde"), help="run one kernel measurement alone (for ncu)")
-    ap.add_argument("--tile-policy", help="fixed tile policy 'update,inverse,lauum' instead of tuning (for ncu)")
+    ap.add_argument("--tile-policy", help="fixed tile policy 'update,inverse' instead of tuning (for ncu)")
     return ap.parse_args()
 
 
@@ -320,8 +320,8 @@ def roofline(A, dist: Dist, tune_policy: bool = True):
     inv_flops = float(S) ** 3
     achieved = inv_flops / t_inv_mixed / 1e12
     roof = {
-        "kernel": "double-float Cholesky + triangular inverse + L^-T L^-1 of A (aj_spd_inverse_mixed: "
-                  "dfchol_panel, dfsyrk_update, df_trtri_step, df_lauum_row)",
+        "kernel": "double-float Cholesky + triangular inverse of A, then L^-T L^-1 on the tensor cores "
+                  "(aj_spd_inverse_mixed: dfchol_panel, dfsyrk_update, df_trtri_step, digit_syrk)",
         "bound": "fp32 (double-float)",
         "achieved": achieved,
         "peak": df_peak,
@@ -487,7 +487,7 @@ def gpu_arm(args, dist: Dist) -> dict:
             "l2": "inputs larger than L2 (w_tilde 722 MB float64 re-read every step)",
             "graph": not args.no_graph,
             "parallelism": f"replicas x{dist.world}",
-            "tile_policy": {"min_64_tiles (update, L^-1, A^-1)": list(tuned["policy"]),
+            "tile_policy": {"min_64_tiles (update, L^-1)": list(tuned["policy"]),
                             "tuned_ms": tuned["ms"], "default_ms": tuned["ms_default"],
                             "candidates_timed": tuned["candidates_timed"]},
         },

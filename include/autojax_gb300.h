@@ -126,13 +126,13 @@ int aj_w_tilde_data(const double* visibilities_real, const double* noise_map_rea
                     size_t workspace_bytes, int precision, void* stream);
 
 /* Tile policy of the double-float factorisation (no reference counterpart).
- * A step of the trailing update, of L^-1 or of the streamed A^-1 runs in
- * 64 x 64 output tiles when it has at least this many of them (per matrix),
- * else in 32 x 32 tiles. Results do not depend on the choice; speed does.
- * Process-wide; set between calls (a captured graph keeps the choice made at
- * capture). autojax_gb300.tune picks the values by timing. */
-int aj_set_tile_policy(int update_min_tiles, int inverse_min_tiles, int lauum_min_tiles);
-int aj_get_tile_policy(int* out3);
+ * A step of the trailing update or of L^-1 runs in 64 x 64 output tiles when
+ * it has at least this many of them (per matrix), else in 32 x 32 tiles.
+ * Results do not depend on the choice; speed does. Process-wide; set between
+ * calls (a captured graph keeps the choice made at capture).
+ * autojax_gb300.tune picks the values by timing. */
+int aj_set_tile_policy(int update_min_tiles, int inverse_min_tiles);
+int aj_get_tile_policy(int* out2);
 
 /* Dirty image (no reference function; the reference reads it from its
  * dataset, tests.py:424-426): out[i] = sum_k noise_k^-2 (Re V_k cos t - Im V_k

@@ -107,7 +107,7 @@ SIGNATURES = {
     "aj_split_f64": (INT, [P, I64, P, P, P]),
     "aj_log_evidence_workspace_size": (SZ, [C.POINTER(Problem), INT, INT]),
     "aj_log_evidence": (INT, [C.POINTER(Problem), INT, INT, P, P, P, P, SZ, P, P]),
-    "aj_set_tile_policy": (INT, [INT, INT, INT]),
+    "aj_set_tile_policy": (INT, [INT, INT]),
     "aj_get_tile_policy": (INT, [P]),
     "aj_dirty_image_workspace_size": (SZ, [I64, I64]),
     "aj_dirty_image": (INT, [P, P, P, P, I64, I64, P, P, SZ, P]),

@@ -1,11 +1,11 @@
 """Autotuner for the tile shapes of the double-float factorisation.
 
-Each step of the trailing update, of L^-1 and of the streamed A^-1 runs in
-64 x 64 or 32 x 32 output tiles; the switch points (minimum 64-tile counts,
+Each step of the trailing update and of L^-1 runs in 64 x 64 or 32 x 32
+output tiles; the switch points (minimum 64-tile counts,
 ``aj_set_tile_policy``) decide how the lanes share the GPU and depend on S,
 on how many matrices run at once and on the GPU.  The results do not depend
 on the choice (the two tile sizes add in the same order), so the tuner only
-times: coordinate descent over the three thresholds, each candidate timed
+times: coordinate descent over the two thresholds, each candidate timed
 with CUDA events on the work the caller passes (an evaluation or a batch).
 """
 
@@ -24,15 +24,14 @@ NEVER = 1 << 30  # a threshold no step reaches: always 32 x 32 tiles
 CANDIDATES = (32, 64, 128, 256, NEVER)
 
 
-def get_tile_policy() -> tuple[int, int, int]:
-    out = (ctypes.c_int * 3)()
+def get_tile_policy() -> tuple[int, int]:
+    out = (ctypes.c_int * 2)()
     _lib.check(_lib.load().aj_get_tile_policy(out), "aj_get_tile_policy")
     return tuple(int(v) for v in out)
 
 
-def set_tile_policy(update_min_tiles: int, inverse_min_tiles: int, lauum_min_tiles: int) -> None:
-    _lib.check(_lib.load().aj_set_tile_policy(int(update_min_tiles), int(inverse_min_tiles), int(lauum_min_tiles)),
-               "aj_set_tile_policy")
+def set_tile_policy(update_min_tiles: int, inverse_min_tiles: int) -> None:
+    _lib.check(_lib.load().aj_set_tile_policy(int(update_min_tiles), int(inverse_min_tiles)), "aj_set_tile_policy")
 
 
 def _time(run, reps: int) -> float:
@@ -93,7 +92,7 @@ def tune_tile_policy(run, candidates=CANDIDATES, reps: int = 4, rounds: int = 2,
     tried = {tuple(best): best_ms}
     for _ in range(rounds):
         improved = False
-        for axis in range(3):
+        for axis in range(2):
             for c in candidates:
                 cand = list(best)
                 cand[axis] = c
@@ -120,7 +119,7 @@ def tune_tile_policy(run, candidates=CANDIDATES, reps: int = 4, rounds: int = 2,
         except OSError:
             pass
     return {"policy": tuple(best), "ms": best_ms, "candidates_timed": len(tried),
-            "ms_default": tried.get((128, 128, 96)), "cached": False}
+            "ms_default": tried.get((128, 128)), "cached": False}
 
 
 __all__ = ["tune_tile_policy", "get_tile_policy", "set_tile_policy", "cache_path", "cache_key", "NEVER", "CANDIDATES"]

@@ -815,73 +815,10 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// Streaming A^-1 = X^T X (X = L^-1 lower): once block row R of X is final,
-// add its contribution X[R][I]^T X[R][J] to every lower tile (I, J), J <= I <= R.
-// Summed over R this is the whole product, so A^-1 builds up while the
-// factorisation and L^-1 are still running instead of after them.  128
-// threads, 8 outputs each (the trailing-update layout).
-__global__ void __launch_bounds__(128)
-    df_lauum_row_kernel(const float* __restrict__ Xh, const float* __restrict__ Xl, float* __restrict__ Ch,
-                        float* __restrict__ Cl, int64_t S, int64_t R) {
-    __shared__ float pih[32][33], pil[32][33], pjh[32][33], pjl[32][33];
-    int64_t ti, tj;
-    lower_tile_df(blockIdx.x, ti, tj);
-    const int64_t r0 = R * DNB, i0 = ti * DNB, j0 = tj * DNB;
-    const int tid = threadIdx.x;
-    const int ty = tid >> 3, tx = tid & 7;  // outputs (i0 + ty + 16 a, j0 + tx + 8 b)
-    df cur[2][4];
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            const int64_t gi = i0 + ty + 16 * a, gj = j0 + tx + 8 * b;
-            const bool in = gi < S && gj < S;
-            cur[a][b] = in ? df{Ch[gi * S + gj], Cl[gi * S + gj]} : df{0.f, 0.f};
-        }
-    // pi[c][x] = X[r0 + c][i0 + x], pj[c][x] = X[r0 + c][j0 + x]
-    for (int e = tid; e < 32 * 32; e += 128) {
-        const int c = e >> 5, x = e & 31;
-        const int64_t r = r0 + c;
-        const bool ii = r < S && i0 + x < S, jj = r < S && j0 + x < S;
-        pih[c][x] = ii ? Xh[r * S + i0 + x] : 0.f;
-        pil[c][x] = ii ? Xl[r * S + i0 + x] : 0.f;
-        pjh[c][x] = jj ? Xh[r * S + j0 + x] : 0.f;
-        pjl[c][x] = jj ? Xl[r * S + j0 + x] : 0.f;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int c8 = 0; c8 < 32; c8 += 8) {
-#pragma unroll
-        for (int c = c8; c < c8 + 8; ++c) {
-            const df x0 = {pih[c][ty], pil[c][ty]}, x1 = {pih[c][ty + 16], pil[c][ty + 16]};
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const df y = {pjh[c][tx + 8 * b], pjl[c][tx + 8 * b]};
-                df_fma_lazy(cur[0][b], x0, y);
-                df_fma_lazy(cur[1][b], x1, y);
-            }
-        }
-#pragma unroll
-        for (int a = 0; a < 2; ++a)
-#pragma unroll
-            for (int b = 0; b < 4; ++b) df_renorm(cur[a][b]);
-    }
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            const int64_t gi = i0 + ty + 16 * a, gj = j0 + tx + 8 * b;
-            if (gi < S && gj < S) {
-                Ch[gi * S + gj] = cur[a][b].hi;
-                Cl[gi * S + gj] = cur[a][b].lo;
-            }
-        }
-}
-
 // ------------------------------------------------- 64 x 64 tile updates
 //
-// The large steps of the trailing update, L^-1 and the streamed A^-1 use
-// 64 x 64 output tiles: 256 threads with 4 x 4 outputs each (rows ty + 16a,
+// The large steps of the trailing update and of L^-1 use 64 x 64 output
+// tiles: 256 threads with 4 x 4 outputs each (rows ty + 16a,
 // columns tx + 16b) read k-major (hi, lo) pairs from shared memory, half a
 // shared load per double-float multiply-add against ~1.5 for the 32 x 32
 // kernels.  The order over k, the operand order and the renormalisation
@@ -1015,42 +952,6 @@ __global__ void __launch_bounds__(256)
             if (gi < S && gj < ncol) {
                 Ih[gi * S + gj] = acc[i][j].hi;
                 Il[gi * S + gj] = acc[i][j].lo;
-            }
-        }
-}
-
-// Streamed A^-1 for block row R of X = L^-1 in 64 x 64 tiles (I, J), J <= I, over the first
-// (R + 1) 32 rows and columns: C[i][j] += sum_c X[R 32 + c][i] X[R 32 + c][j]
-__global__ void __launch_bounds__(256)
-    df_lauum64_kernel(const float* __restrict__ Xh, const float* __restrict__ Xl, float* __restrict__ Ch,
-                      float* __restrict__ Cl, int64_t S, int64_t R) {
-    __shared__ Tile64 t;
-    int64_t ti, tj;
-    lower_tile_df(blockIdx.x, ti, tj);
-    const int64_t lim = (R + 1) * DNB < S ? (R + 1) * DNB : S;  // X row block R is zero past column lim
-    const int64_t i0 = ti * T64, j0 = tj * T64, r0 = R * DNB;
-    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
-    df cur[4][4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int64_t gi = i0 + ty + 16 * i, gj = j0 + tx + 16 * j;
-            const bool in = gi < lim && gj < lim;
-            cur[i][j] = in ? df{Ch[gi * S + gj], Cl[gi * S + gj]} : df{0.f, 0.f};
-        }
-    load_cols(t.a, Xh, Xl, S, r0, i0);
-    load_cols(t.b, Xh, Xl, S, r0, j0);
-    __syncthreads();
-    tile64_mac(t, cur, ty, tx);
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int64_t gi = i0 + ty + 16 * i, gj = j0 + tx + 16 * j;
-            if (gi < lim && gj < lim) {
-                Ch[gi * S + gj] = cur[i][j].hi;
-                Cl[gi * S + gj] = cur[i][j].lo;
             }
         }
 }
@@ -1316,7 +1217,7 @@ static DfMats mats_of(DfSpd* const* w, int count) {
 // When a step switches from 32 x 32 to 64 x 64 tiles: the minimum number of
 // 64 x 64 output tiles per matrix (below it the 32 x 32 kernels, with 4x the
 // blocks, fill the GPU better).  Set by aj_set_tile_policy (the autotuner).
-static int g_tile64_min[3] = {128, 128, 96};  // trailing update, L^-1 step, A^-1 row
+static int g_tile64_min[2] = {128, 128};  // trailing update, L^-1 step
 
 // L (in w[z]) = chol(A[z]) for z < count (1 or 2), and L^-1 for z < n_inverse; A given as planes
 // (copied unless it is w's own L).  With `prepared` the caller has already put each A's lower
@@ -1360,12 +1261,11 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
     Lanes* lanes = nullptr;
     AJ_TRY(lanes_for(st, &lanes));
     Lanes& ln = *lanes;
-    // A^-1 = L^-T L^-1: on the tensor cores after the factorisation when matrix 0 has the scratch
-    // for it, otherwise streamed in double-float on lane 4, one finished block row of L^-1 at a time
-    // (the tensor-core product streamed by 256-row slabs on lane 4 measured slower in the batch,
-    // 572 against 596 evaluations/s, and no faster alone: its CTAs, one an SM, crowd the panels)
-    const bool tc_ainv = AIh && w[0]->tcws;
-    const int nlanes = (AIh && !tc_ainv) ? 5 : 2 + n_inverse;  // lanes 2 .. 1 + n_inverse: L^-1; 4: A^-1
+    // A^-1 = L^-T L^-1 on the tensor cores once the lanes have joined (the product streamed by
+    // 256-row slabs of L^-1 beside the factorisation measured slower in the batch, 572 against 596
+    // evaluations/s, and no faster alone: its CTAs, one an SM, crowd the panels)
+    if (AIh && !w[0]->tcws) return AJ_ERR_ARG;
+    const int nlanes = 2 + n_inverse;  // lanes 2 .. 1 + n_inverse for L^-1
     AJ_TRY(lanes_fork(ln, st, nlanes));
     cudaStream_t crit = ln.s[0], bulk = ln.s[1];
     // each matrix's L^-1 on its own lane: a view of m whose slot 0 is matrix z
@@ -1397,24 +1297,10 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
         dfchol_panel_kernel<<<dim3(g, count), PANEL_THREADS, PANEL_DYN_SMEM, crit>>>(m, S, k0, kb > 0 ? 1 : 0, info);
         return check_launch();
     };
-    // A^-1 of matrix 0, one final block row of its L^-1 at a time
-    auto lauum_row = [&](int64_t R, cudaStream_t on) {
-        const int64_t lim = (R + 1) * DNB < S ? (R + 1) * DNB : S;
-        const int64_t nT = (lim + T64 - 1) / T64;
-        if (nT * (nT + 1) / 2 >= g_tile64_min[2]) {
-            df_lauum64_kernel<<<(unsigned)(nT * (nT + 1) / 2), 256, 0, on>>>(w[0]->Ih, w[0]->Il, AIh, AIl, S, R);
-        } else {
-            const int64_t tiles = (R + 1) * (R + 2) / 2;
-            df_lauum_row_kernel<<<(unsigned)tiles, 128, 0, on>>>(w[0]->Ih, w[0]->Il, AIh, AIl, S, R);
-        }
-        return check_launch();
-    };
     // Step kb: panel kb + 1 applies panel kb's update to its own block column,
     // so it only has to wait for the bulk update of step kb - 1 (which reached
     // that column); the bulk update of step kb covers the columns after it.
-    cudaStream_t lau = ln.s[4];
     AJ_TRY(panel(0));
-    if (AIh && !tc_ainv && nbt == 1) AJ_TRY(lauum_row(0, crit));
     bool rest_prev = false;
     for (int64_t kb = 0; kb + 1 < nbt; ++kb) {
         const int64_t k0 = kb * DNB;
@@ -1451,13 +1337,6 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
                     AJ_LAUNCHED();
                 }
             }
-            // block row 0 of L^-1 is final since panel 0, block row kb + 1 after this step
-            if (AIh && !tc_ainv) {
-                AJ_TRY(lane_signal(ln, kEvRow, 2));
-                AJ_TRY(lane_wait(ln, 4, kEvRow));
-                if (kb == 0) AJ_TRY(lauum_row(0, lau));
-                AJ_TRY(lauum_row(kb + 1, lau));
-            }
         }
     }
     df_store_diag_kernel<<<dim3((unsigned)nbt, count), 256, 0, crit>>>(m, S);
@@ -1472,7 +1351,7 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
         AJ_LAUNCHED();
     }
     AJ_TRY(lanes_join(ln, st, nlanes));
-    if (tc_ainv) AJ_TRY(tc_lauum(w[0]->Ih, w[0]->Il, S, AIh, AIl, w[0]->tcws, w[0]->tcws_bytes, st));
+    if (AIh) AJ_TRY(tc_lauum(w[0]->Ih, w[0]->Il, S, AIh, AIl, w[0]->tcws, w[0]->tcws_bytes, st));
     return AIh ? df_mirror_lower(AIh, AIl, S, st) : AJ_OK;
 }
 
@@ -1532,17 +1411,16 @@ using namespace aj;
 
 extern "C" {
 
-int aj_set_tile_policy(int update_min_tiles, int inverse_min_tiles, int lauum_min_tiles) {
-    if (update_min_tiles < 1 || inverse_min_tiles < 1 || lauum_min_tiles < 1) return AJ_ERR_ARG;
+int aj_set_tile_policy(int update_min_tiles, int inverse_min_tiles) {
+    if (update_min_tiles < 1 || inverse_min_tiles < 1) return AJ_ERR_ARG;
     aj::g_tile64_min[0] = update_min_tiles;
     aj::g_tile64_min[1] = inverse_min_tiles;
-    aj::g_tile64_min[2] = lauum_min_tiles;
     return AJ_OK;
 }
 
-int aj_get_tile_policy(int* out3) {
-    if (!out3) return AJ_ERR_ARG;
-    for (int i = 0; i < 3; ++i) out3[i] = aj::g_tile64_min[i];
+int aj_get_tile_policy(int* out2) {
+    if (!out2) return AJ_ERR_ARG;
+    for (int i = 0; i < 2; ++i) out2[i] = aj::g_tile64_min[i];
     return AJ_OK;
 }
 

@@ -14,15 +14,15 @@ def test_cached_policy_is_used_without_timing(tmp_path, monkeypatch):
     cache = tmp_path / "tile_policy.json"
     monkeypatch.setenv("AUTOJAX_GB300_CACHE", str(cache))
     assert tune.cache_path() == cache
-    cache.write_text(json.dumps({"gpu|S=1500": [64, 96, 32]}))
+    cache.write_text(json.dumps({"gpu|S=1500": [64, 96]}))
     saved = tune.get_tile_policy()
     try:
         def never_called():
             raise AssertionError("a cached key must not be timed")
 
         out = tune.tune_tile_policy(never_called, key="gpu|S=1500")
-        assert out["cached"] and out["policy"] == (64, 96, 32)
-        assert tune.get_tile_policy() == (64, 96, 32)
+        assert out["cached"] and out["policy"] == (64, 96)
+        assert tune.get_tile_policy() == (64, 96)
     finally:
         tune.set_tile_policy(*saved)
 
@@ -31,12 +31,12 @@ def test_policy_rejects_non_positive_thresholds():
     from autojax_gb300 import _lib, tune
 
     with pytest.raises(Exception):
-        tune.set_tile_policy(0, 1, 1)
-    assert _lib.load().aj_set_tile_policy(1, 1, -3) == _lib.AJ_ERR_ARG
+        tune.set_tile_policy(0, 1)
+    assert _lib.load().aj_set_tile_policy(1, -3) == _lib.AJ_ERR_ARG
 
 
 def test_descent_finds_the_fastest_policy_and_caches_it(tmp_path, monkeypatch):
-    """Coordinate descent over the three thresholds on a synthetic cost with one minimum: the
+    """Coordinate descent over the two thresholds on a synthetic cost with one minimum: the
     tuner sets it, times each candidate once, calls ``prepare`` after every policy it sets and
     writes the result under its key."""
     import math
@@ -45,7 +45,7 @@ def test_descent_finds_the_fastest_policy_and_caches_it(tmp_path, monkeypatch):
 
     cache = tmp_path / "tile_policy.json"
     monkeypatch.setenv("AUTOJAX_GB300_CACHE", str(cache))
-    target = (64, tune.NEVER, 128)
+    target = (64, tune.NEVER)
 
     def cost(policy):
         return sum(abs(math.log2(p) - math.log2(t)) for p, t in zip(policy, target))
