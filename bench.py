@@ -245,10 +245,10 @@ def time_region(fn, steps: int, dist: Dist, name: str = "region") -> float:
 
 
 # DRAM bytes (read + write) of one aj_spd_inverse_mixed call at S = 1,500, summed
-# over its launches in a warm-cache ncu capture of one call (16.0 MB read,
-# 56.9 MB written): the group's working set, 7 double-float S x S planes
-# (63 MB), stays in L2.
-ROOFLINE_TRAFFIC_BYTES = 72.9e6
+# over its launches in a warm-cache ncu capture of one call (9.9 MB read,
+# 108.3 MB written): the group's working set, the double-float S x S planes and
+# the tensor-core product's digit planes (74 MB together), stays in L2.
+ROOFLINE_TRAFFIC_BYTES = 118.2e6
 
 
 def roofline(A, dist: Dist, tune_policy: bool = True):

@@ -81,4 +81,42 @@ __device__ __forceinline__ df df_add(df a, df b) {
 
 __device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
 
+// a * b, renormalised
+__device__ __forceinline__ df dfmul(df a, df b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return df_norm({p, e});
+}
+
+__device__ __forceinline__ df dfsqrt(df d) {
+    const float y = sqrtf(d.hi);
+    if (!(y > 0.f)) return {y, 0.f};
+    const float p = y * y;
+    const float e = fmaf(y, y, -p);
+    const float diff = ((d.hi - p) - e) + d.lo;
+    return df_norm({y, diff * (0.5f / y)});
+}
+
+__device__ __forceinline__ df dfrcp(df l) {
+    const float r0 = 1.0f / l.hi;
+    const float q = l.hi * r0;
+    const float qe = fmaf(l.hi, r0, -q) + l.lo * r0;
+    const float one_minus = (1.0f - q) - qe;
+    return df_norm({r0, r0 * one_minus});
+}
+
+// 1/sqrt(d) to double-float accuracy: hardware rsqrt, one float Newton step,
+// one double-float Newton step (no divisions on the critical path)
+__device__ __forceinline__ df dfrsqrt(df d) {
+    float r = rsqrtf(d.hi);
+    r = r * fmaf(-0.5f * d.hi * r, r, 1.5f);
+    const float q = r * r;
+    const float qe = fmaf(r, r, -q);
+    const df t = dfmul(d, {q, qe});
+    const float h = (1.0f - t.hi) - t.lo;
+    return df_norm({r, 0.5f * r * h});
+}
+
 }  // namespace aj

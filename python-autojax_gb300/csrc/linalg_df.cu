@@ -44,43 +44,6 @@ __device__ __forceinline__ T pick(T const (&a)[2], int z) {
     return z ? a[1] : a[0];
 }
 
-__device__ __forceinline__ df dfmul(df a, df b) {
-    const float p = a.hi * b.hi;
-    float e = fmaf(a.hi, b.hi, -p);
-    e = fmaf(a.hi, b.lo, e);
-    e = fmaf(a.lo, b.hi, e);
-    return df_norm({p, e});
-}
-
-__device__ __forceinline__ df dfsqrt(df d) {
-    const float y = sqrtf(d.hi);
-    if (!(y > 0.f)) return {y, 0.f};
-    const float p = y * y;
-    const float e = fmaf(y, y, -p);
-    const float diff = ((d.hi - p) - e) + d.lo;
-    return df_norm({y, diff * (0.5f / y)});
-}
-
-__device__ __forceinline__ df dfrcp(df l) {
-    const float r0 = 1.0f / l.hi;
-    const float q = l.hi * r0;
-    const float qe = fmaf(l.hi, r0, -q) + l.lo * r0;
-    const float one_minus = (1.0f - q) - qe;
-    return df_norm({r0, r0 * one_minus});
-}
-
-// 1/sqrt(d) to double-float accuracy: hardware rsqrt, one float Newton step,
-// one double-float Newton step (no divisions on the critical path)
-__device__ __forceinline__ df dfrsqrt(df d) {
-    float r = rsqrtf(d.hi);
-    r = r * fmaf(-0.5f * d.hi * r, r, 1.5f);
-    const float q = r * r;
-    const float qe = fmaf(r, r, -q);
-    const df t = dfmul(d, {q, qe});
-    const float h = (1.0f - t.hi) - t.lo;
-    return df_norm({r, 0.5f * r * h});
-}
-
 // tile t of the lower triangle, row-major: (bi, bj) with bj <= bi.  The float
 // square root is exact enough for a first guess (t < 2^24); the loops fix it.
 __device__ __forceinline__ void lower_tile_df(int64_t t, int64_t& bi, int64_t& bj) {
@@ -628,13 +591,14 @@ __global__ void __launch_bounds__(PANEL_THREADS)
 // Trailing update of one Cholesky step past the next block column (which the
 // next panel kernel updates itself): C (lower 32 x 32 tiles of the trailing
 // matrix, tile columns >= 1) -= P P^T with P the solved panel.  128 threads,
-// 8 outputs each; small register and shared footprint so several blocks share
+// 8 outputs each, operands as (hi, lo) pairs (6 shared loads per 8
+// multiply-adds); small register and shared footprint so several blocks share
 // an SM and the late, small steps still fill the GPU.
 __global__ void __launch_bounds__(128)
     dfsyrk_update_kernel(DfMats mats, int64_t S, int64_t k0) {
     float* __restrict__ Lh = pick(mats.Lh, blockIdx.y);
     float* __restrict__ Ll = pick(mats.Ll, blockIdx.y);
-    __shared__ float pih[32][33], pil[32][33], pjh[32][33], pjl[32][33];
+    __shared__ float2 pi[32][33], pj[32][33];  // (hi, lo) of the panel rows of tile rows i and j
     const int64_t r0 = k0 + DNB;
     int64_t ti, tj;
     lower_tile_df(blockIdx.x, ti, tj);
@@ -656,10 +620,8 @@ __global__ void __launch_bounds__(128)
     for (int e = tid; e < 32 * 32; e += 128) {
         const int a = e >> 5, b = e & 31;
         const bool ii = i0 + a < S, jj = j0 + a < S;
-        pih[a][b] = ii ? Lh[(i0 + a) * S + k0 + b] : 0.f;
-        pil[a][b] = ii ? Ll[(i0 + a) * S + k0 + b] : 0.f;
-        pjh[a][b] = jj ? Lh[(j0 + a) * S + k0 + b] : 0.f;
-        pjl[a][b] = jj ? Ll[(j0 + a) * S + k0 + b] : 0.f;
+        pi[a][b] = ii ? make_float2(Lh[(i0 + a) * S + k0 + b], Ll[(i0 + a) * S + k0 + b]) : make_float2(0.f, 0.f);
+        pj[a][b] = jj ? make_float2(Lh[(j0 + a) * S + k0 + b], Ll[(j0 + a) * S + k0 + b]) : make_float2(0.f, 0.f);
     }
     __syncthreads();
     df acc[2][4];
@@ -671,12 +633,12 @@ __global__ void __launch_bounds__(128)
     for (int k8 = 0; k8 < 32; k8 += 8) {
 #pragma unroll
         for (int k = k8; k < k8 + 8; ++k) {
-            const df x0 = {pih[ty][k], pil[ty][k]}, x1 = {pih[ty + 16][k], pil[ty + 16][k]};
+            const float2 x0 = pi[ty][k], x1 = pi[ty + 16][k];
 #pragma unroll
             for (int b = 0; b < 4; ++b) {
-                const df y = {pjh[tx + 8 * b][k], pjl[tx + 8 * b][k]};
-                df_fma_lazy(acc[0][b], x0, y);
-                df_fma_lazy(acc[1][b], x1, y);
+                const float2 y = pj[tx + 8 * b][k];
+                df_fma_lazy(acc[0][b], {x0.x, x0.y}, {y.x, y.y});
+                df_fma_lazy(acc[1][b], {x1.x, x1.y}, {y.x, y.y});
             }
         }
 #pragma unroll
@@ -737,7 +699,14 @@ __global__ void df_logdet_kernel(const double* __restrict__ piv0, const double* 
 
 // ---------------------------------------------------- triangular inverse
 
-// see trtri_step_kernel (linalg.cu): accumulate L[ti][kb] X[kb][tj]; block row kb + 1 applies -dinv
+// see trtri_step_kernel (linalg.cu): accumulate L[ti][kb] X[kb][tj]; block row kb + 1 applies -dinv.
+// 256 threads, 4 outputs each (row r, columns q + 8t): the L^-1 steps trail the factorisation one
+// a panel, so a step's latency counts as much as its throughput (128 threads with 8 outputs each
+// measured 2.605 against 2.532 ms an evaluation).  Operands as (hi, lo) pairs in shared memory.
+// Each output adds over k in the order and with the renormalisation points of df_trtri64_kernel,
+// so the two give the same bits.  Block row kb + 1 then multiplies by the diagonal block's inverse
+// (lower triangular: the terms past the diagonal are exact zeros), unrolled, one lazy chain per
+// output.
 __global__ void __launch_bounds__(256)
     df_trtri_step_kernel(DfMats mats, int64_t S, int64_t kb) {
     const float* __restrict__ Lh = pick(mats.Lh, blockIdx.y);
@@ -746,37 +715,38 @@ __global__ void __launch_bounds__(256)
     float* __restrict__ Il = pick(mats.Il, blockIdx.y);
     const float* __restrict__ dh = pick(mats.dh, blockIdx.y);
     const float* __restrict__ dl = pick(mats.dl, blockIdx.y);
-    __shared__ float ah[32][33], al[32][33], bh[32][33], bl[32][33];
+    __shared__ float2 as[32][33], bs[32][33];  // as[r][k] = L[i0 + r][p0 + k], bs[k][c] = X[p0 + k][j0 + c]
     const int64_t nbt = (S + DNB - 1) / DNB;
     const int64_t ncol = kb + 1;
     const int64_t ti = kb + 1 + blockIdx.x / ncol, tj = blockIdx.x % ncol;
     if (ti >= nbt) return;
     const int tid = threadIdx.x;
     const int64_t i0 = ti * DNB, j0 = tj * DNB, p0 = kb * DNB;
-    for (int e = tid; e < DNB * DNB; e += 256) {
-        const int r = e / DNB, c = e % DNB;
-        const bool ina = i0 + r < S && p0 + c < S, inb = p0 + r < S && j0 + c < S;
-        ah[r][c] = ina ? Lh[(i0 + r) * S + p0 + c] : 0.f;
-        al[r][c] = ina ? Ll[(i0 + r) * S + p0 + c] : 0.f;
-        bh[r][c] = inb ? Ih[(p0 + r) * S + j0 + c] : 0.f;
-        bl[r][c] = inb ? Il[(p0 + r) * S + j0 + c] : 0.f;
-    }
-    __syncthreads();
     const int r = tid >> 3, q = tid & 7;
     df acc[4];
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
-        const int c = q + 8 * t;
-        const bool in = i0 + r < S && j0 + c < S;
-        acc[t] = in ? df{Ih[(i0 + r) * S + j0 + c], Il[(i0 + r) * S + j0 + c]} : df{0.f, 0.f};
+        const int64_t gi = i0 + r, gj = j0 + q + 8 * t;
+        const bool in = gi < S && gj < S;
+        acc[t] = in ? df{Ih[gi * S + gj], Il[gi * S + gj]} : df{0.f, 0.f};
     }
+    for (int e = tid; e < DNB * DNB; e += 256) {
+        const int rr = e / DNB, c = e % DNB;
+        const bool ina = i0 + rr < S && p0 + c < S, inb = p0 + rr < S && j0 + c < S;
+        as[rr][c] = ina ? make_float2(Lh[(i0 + rr) * S + p0 + c], Ll[(i0 + rr) * S + p0 + c]) : make_float2(0.f, 0.f);
+        bs[rr][c] = inb ? make_float2(Ih[(p0 + rr) * S + j0 + c], Il[(p0 + rr) * S + j0 + c]) : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
 #pragma unroll
-    for (int p0 = 0; p0 < DNB; p0 += 8) {
+    for (int k8 = 0; k8 < DNB; k8 += 8) {
 #pragma unroll
-        for (int p = p0; p < p0 + 8; ++p) {
-            const df x = {ah[r][p], al[r][p]};
+        for (int k = k8; k < k8 + 8; ++k) {
+            const float2 x = as[r][k];
 #pragma unroll
-            for (int t = 0; t < 4; ++t) df_fma_lazy(acc[t], x, {bh[p][q + 8 * t], bl[p][q + 8 * t]});
+            for (int t = 0; t < 4; ++t) {
+                const float2 y = bs[k][q + 8 * t];
+                df_fma_lazy(acc[t], {x.x, x.y}, {y.x, y.y});
+            }
         }
 #pragma unroll
         for (int t = 0; t < 4; ++t) df_renorm(acc[t]);
@@ -784,33 +754,42 @@ __global__ void __launch_bounds__(256)
     if (ti != kb + 1) {
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
-            const int c = q + 8 * t;
-            if (i0 + r < S && j0 + c < S) {
-                Ih[(i0 + r) * S + j0 + c] = acc[t].hi;
-                Il[(i0 + r) * S + j0 + c] = acc[t].lo;
+            const int64_t gi = i0 + r, gj = j0 + q + 8 * t;
+            if (gi < S && gj < S) {
+                Ih[gi * S + gj] = acc[t].hi;
+                Il[gi * S + gj] = acc[t].lo;
             }
         }
         return;
     }
+    // X[kb + 1 block][tj] = -dinv_{kb+1} acc: acc to shared memory (as), dinv into bs
     __syncthreads();
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        ah[r][q + 8 * t] = acc[t].hi;
-        al[r][q + 8 * t] = acc[t].lo;
-    }
-    for (int e = tid; e < DNB * DNB; e += 256) {
-        bh[e / DNB][e % DNB] = dh[(kb + 1) * DNB * DNB + e];
-        bl[e / DNB][e % DNB] = dl[(kb + 1) * DNB * DNB + e];
-    }
+    for (int t = 0; t < 4; ++t) as[r][q + 8 * t] = make_float2(acc[t].hi, acc[t].lo);
+    for (int e = tid; e < DNB * DNB; e += 256)
+        bs[e / DNB][e % DNB] = make_float2(dh[(kb + 1) * DNB * DNB + e], dl[(kb + 1) * DNB * DNB + e]);
     __syncthreads();
+    df out[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+    for (int p8 = 0; p8 < DNB; p8 += 8) {
+#pragma unroll
+        for (int p = p8; p < p8 + 8; ++p) {
+            const float2 d = bs[r][p];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const float2 y = as[p][q + 8 * t];
+                df_fma_lazy(out[t], {d.x, d.y}, {y.x, y.y});
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < 4; ++t) df_renorm(out[t]);
+    }
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
-        const int c = q + 8 * t;
-        df s = {0.f, 0.f};
-        for (int p = 0; p <= r; ++p) df_fma_acc(s, {bh[r][p], bl[r][p]}, {ah[p][c], al[p][c]});
-        if (i0 + r < S && j0 + c < S) {
-            Ih[(i0 + r) * S + j0 + c] = -s.hi;
-            Il[(i0 + r) * S + j0 + c] = -s.lo;
+        const int64_t gi = i0 + r, gj = j0 + q + 8 * t;
+        if (gi < S && gj < S) {
+            Ih[gi * S + gj] = -out[t].hi;
+            Il[gi * S + gj] = -out[t].lo;
         }
     }
 }
