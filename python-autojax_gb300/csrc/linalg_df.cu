@@ -257,9 +257,16 @@ static_assert(PANEL_THREADS >= 3 * 32 && PANEL_THREADS % 128 == 0 && DNB % PANEL
 constexpr int PRE_DIGITS = 6;  // 8-bit digits per double-float value in the tensor-core pre-update
 constexpr int PRE_LEVELS = 7;  // digit-product levels i + j kept
 constexpr int PRE_KS = DNB + 8;  // bf16 row stride of the digit planes: conflict-free fragment loads
-// previous-panel rows as (hi, lo) pairs (the pivot block's 32 and this block's 64), then their
-// digit planes
-constexpr size_t PANEL_DYN_SMEM = sizeof(float2) * (32 + 64) * (32 + 1) + sizeof(uint16_t) * PRE_DIGITS * 3 * DNB * PRE_KS;
+// Panel rows a block solves besides the pivot block.  A panel block holds a whole SM while most of
+// its threads wait on the pivot chain: 128 rows (half the blocks) measured 2.604 against 2.462 ms
+// an evaluation (the chain's steps grow) and 608 against 596 evaluations/s batched.
+constexpr int PANEL_ROWS = 64;
+constexpr int PANEL_NROW = DNB + PANEL_ROWS;  // a block's rows: the pivot block's, then its panel rows
+static_assert(PANEL_NROW >= 3 * DNB, "block 0 keeps L_kk^-1 and a scratch block in the panel-row space");
+// previous-panel rows as (hi, lo) pairs (the pivot block's 32 and this block's panel rows), then
+// their digit planes
+constexpr size_t PANEL_DYN_SMEM =
+    sizeof(float2) * PANEL_NROW * (DNB + 1) + sizeof(uint16_t) * PRE_DIGITS * PANEL_NROW * PRE_KS;
 
 // x 2^k for k <= 252, exact unless the result leaves the normal range (two power-of-two factors
 // built from their exponent bits, each within the float range)
@@ -292,18 +299,18 @@ __global__ void __launch_bounds__(PANEL_THREADS)
     float* __restrict__ fh = pick(mats.fh, z) + kb * DNB * DNB;
     float* __restrict__ fl = pick(mats.fl, z) + kb * DNB * DNB;
     double* __restrict__ piv = pick(mats.piv, z);
-    // the block's rows: 0 .. 31 the pivot block (lower triangle), 32 .. 95 the panel rows
-    __shared__ float ph[3 * DNB][DNB + 1], pl[3 * DNB][DNB + 1];
+    // the block's rows: 0 .. 31 the pivot block (lower triangle), then PANEL_ROWS panel rows
+    __shared__ float ph[PANEL_NROW][DNB + 1], pl[PANEL_NROW][DNB + 1];
     __shared__ float rh[DNB], rl[DNB];
     extern __shared__ float2 panel_dyn[];
     float2(*pdf)[DNB + 1] = reinterpret_cast<float2(*)[DNB + 1]>(panel_dyn);                    // P_k: 32 rows
-    float2(*prf)[DNB + 1] = reinterpret_cast<float2(*)[DNB + 1]>(panel_dyn + DNB * (DNB + 1));  // P_r: 64 rows
-    uint16_t* xd = reinterpret_cast<uint16_t*>(panel_dyn + 3 * DNB * (DNB + 1));  // digits [i][row][k]
-    __shared__ int pexp[3 * DNB];  // row scales 2^e of the pre-update
+    float2(*prf)[DNB + 1] = reinterpret_cast<float2(*)[DNB + 1]>(panel_dyn + DNB * (DNB + 1));  // P_r
+    uint16_t* xd = reinterpret_cast<uint16_t*>(panel_dyn + PANEL_NROW * (DNB + 1));  // digits [i][row][k]
+    __shared__ int pexp[PANEL_NROW];  // row scales 2^e of the pre-update
     __shared__ int bad;
     const int tid = threadIdx.x;
     const bool rows = blockIdx.x > 0;
-    const int nrow = rows ? 3 * DNB : DNB;
+    const int nrow = rows ? PANEL_NROW : DNB;
     const int64_t nb = (S - k0) < DNB ? (S - k0) : DNB;
     const int64_t kp = k0 - DNB;  // the previous panel's first column (pre only)
     if (tid == 0) bad = 0;
@@ -326,9 +333,9 @@ __global__ void __launch_bounds__(PANEL_THREADS)
         }
     }
     // panel rows are loaded up front so their latency overlaps the factorisation
-    const int64_t r0 = k0 + DNB + (int64_t)(blockIdx.x - 1) * 64;
+    const int64_t r0 = k0 + DNB + (int64_t)(blockIdx.x - 1) * PANEL_ROWS;
     if (rows) {
-        for (int e = tid; e < 64 * DNB; e += PANEL_THREADS) {
+        for (int e = tid; e < PANEL_ROWS * DNB; e += PANEL_THREADS) {
             const int i = e / DNB, j = e % DNB;
             const int64_t r = r0 + i;
             const bool in = r < S && j < nb;
@@ -360,7 +367,7 @@ __global__ void __launch_bounds__(PANEL_THREADS)
 #pragma unroll
             for (int i = 0; i < PRE_DIGITS; ++i) {
                 const float d = rintf(t.hi);  // an integer of at most 8 bits: its bf16 is the top half
-                xd[(i * 3 * DNB + r) * PRE_KS + lane] = (uint16_t)(__float_as_uint(d) >> 16);
+                xd[(i * PANEL_NROW + r) * PRE_KS + lane] = (uint16_t)(__float_as_uint(d) >> 16);
                 float hs, he;
                 two_sum(t.hi - d, t.lo, hs, he);
                 t = {hs * 256.f, he * 256.f};
@@ -381,8 +388,8 @@ __global__ void __launch_bounds__(PANEL_THREADS)
 #pragma unroll
                 for (int j = 0; j < PRE_DIGITS; ++j) {
                     if (i + j >= PRE_LEVELS) continue;
-                    const uint16_t* A = xd + i * 3 * DNB * PRE_KS;
-                    const uint16_t* Bm = xd + j * 3 * DNB * PRE_KS;
+                    const uint16_t* A = xd + i * PANEL_NROW * PRE_KS;
+                    const uint16_t* Bm = xd + j * PANEL_NROW * PRE_KS;
 #pragma unroll
                     for (int ks = 0; ks < DNB; ks += 16) {
                         uint32_t a[4], b[2];
@@ -500,7 +507,7 @@ __global__ void __launch_bounds__(PANEL_THREADS)
         {
             // rows j0 + 8 .. 31 of the pivot block, then the panel rows
             const int npiv = DNB - j0 - PANEL_SP;
-            if (tid < npiv + (rows ? 64 : 0)) {
+            if (tid < npiv + (rows ? PANEL_ROWS : 0)) {
                 const int x = tid < npiv ? j0 + PANEL_SP + tid : DNB + (tid - npiv);
                 df y[PANEL_SP];
 #pragma unroll
@@ -578,7 +585,7 @@ __global__ void __launch_bounds__(PANEL_THREADS)
         }
         return;
     }
-    for (int e = tid; e < 64 * DNB; e += PANEL_THREADS) {
+    for (int e = tid; e < PANEL_ROWS * DNB; e += PANEL_THREADS) {
         const int i = e / DNB, j = e % DNB;
         const int64_t r = r0 + i;
         if (r < S && j < nb) {
@@ -1272,7 +1279,7 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
     auto panel = [&](int64_t kb) {
         const int64_t k0 = kb * DNB;
         const int64_t below = S - k0 - DNB;
-        const unsigned g = 1 + (unsigned)(below > 0 ? (below + 63) / 64 : 0);
+        const unsigned g = 1 + (unsigned)(below > 0 ? (below + PANEL_ROWS - 1) / PANEL_ROWS : 0);
         dfchol_panel_kernel<<<dim3(g, count), PANEL_THREADS, PANEL_DYN_SMEM, crit>>>(m, S, k0, kb > 0 ? 1 : 0, info);
         return check_launch();
     };
