@@ -163,21 +163,48 @@ __device__ __forceinline__ void store_row(float* __restrict__ oh, float* __restr
 // One CTA per lower tile; Rc rows of digits (a multiple of kGroupRows).  The product is scaled by
 // *scale_dev (s^2 2^-(2 first bits)) and, with exps, by 2^(e_i + e_j) per entry (digits of column
 // i cut at its own power of two).  With tri, a digit row k is zero for k < i (the panel is an upper
-// triangle, as the transpose of L^-1 is): a tile starts at the group holding its first row.
+// triangle, as the transpose of L^-1 is): a tile starts at the group holding its first row.  The
+// tiles of the first split_rows row tiles (the ones with the most groups then) are split in two:
+// their CTA sums the first half of the groups into out, and one of the nI (nI + 1)-plus CTAs the
+// second half into out2 (the caller adds out2 to out).
 template <int ND>
 __global__ void __launch_bounds__(kThreads, 1)
     digit_syrk_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                       int64_t Rc, int64_t M, int64_t Mp, float* __restrict__ out_h, float* __restrict__ out_l,
                       int64_t ld, const float* __restrict__ scale_dev, const int* __restrict__ exps, int tri,
-                      int accumulate, int* __restrict__ err) {
+                      int split_rows, float* __restrict__ out2_h, float* __restrict__ out2_l, int accumulate,
+                      int* __restrict__ err) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     Shared* sh = reinterpret_cast<Shared*>(base + size_t(kStages) * Cut<ND>::kStageBytes);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int64_t I, J;
-    tile_of(blockIdx.x, Mp / BM, I, J);
-    const int g0 = tri ? static_cast<int>(max(I * BM, J * BN) / kGroupRows) : 0;
-    const int ngroups = static_cast<int>(Rc / kGroupRows) - g0;  // groups this tile sums, from g0
+    const int64_t nI = Mp / BM, ntiles = nI * (nI + 1);
+    int part = 0;  // 1: the second half of a split tile
+    if (blockIdx.x < ntiles) {
+        tile_of(blockIdx.x, nI, I, J);
+    } else {
+        int64_t e = blockIdx.x - ntiles;  // split tiles in row-major order: 2I + 2 in row tile I
+        I = 0;
+        while (e >= 2 * I + 2) {
+            e -= 2 * I + 2;
+            ++I;
+        }
+        J = e;
+        part = 1;
+    }
+    int g0 = tri ? static_cast<int>(max(I * BM, J * BN) / kGroupRows) : 0;
+    int gend = static_cast<int>(Rc / kGroupRows);
+    if (I < split_rows) {
+        const int gmid = g0 + (gend - g0) / 2;
+        if (part)
+            g0 = gmid;
+        else
+            gend = gmid;
+    }
+    float* __restrict__ oh = part ? out2_h : out_h;
+    float* __restrict__ ol = part ? out2_l : out_l;
+    const int ngroups = gend - g0;  // groups this CTA sums, from g0
     const int nstages = ngroups * kStagesPerGroup;
     const int it0 = g0 * kStagesPerGroup;  // the first stage's k slab
 
@@ -308,7 +335,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         if (!*abort) {
             const int64_t gi = I * BM + q * 32 + lane;
-            store_row(out_h, out_l, ld, M, gi, J * BN, h, l, *scale_dev, exps, accumulate);
+            store_row(oh, ol, ld, M, gi, J * BN, h, l, *scale_dev, exps, accumulate);
         }
     }
     tc_fence_before();
@@ -442,7 +469,8 @@ int set_smem_attr() {
 // (kDigits or kInvDigits) digit planes.
 template <int ND>
 int launch_syrk(const void* D, int64_t Rc, int64_t M, int64_t Mp, float* oh, float* ol, int64_t ld,
-                const float* scale_dev, const int* exps, int tri, int accumulate, int* err, cudaStream_t st) {
+                const float* scale_dev, const int* exps, int tri, int accumulate, int* err, cudaStream_t st,
+                int split_rows = 0, float* o2h = nullptr, float* o2l = nullptr) {
     if (Rc <= 0 || Rc % kGroupRows != 0 || Mp % BM != 0 || Mp < M) return AJ_ERR_ARG;
     if (reinterpret_cast<uintptr_t>(D) % 16 != 0) return AJ_ERR_ARG;
     CUtensorMap ma, mb;
@@ -450,9 +478,10 @@ int launch_syrk(const void* D, int64_t Rc, int64_t M, int64_t Mp, float* oh, flo
     AJ_TRY(make_map(&mb, D, Rc, Mp, BN, ND));
     AJ_TRY(set_smem_attr<ND>());
     const int64_t nI = Mp / BM;
-    const int64_t tiles = nI * (nI + 1);
+    if (split_rows < 0 || split_rows > nI || (split_rows > 0 && (!o2h || !o2l))) return AJ_ERR_ARG;
+    const int64_t tiles = nI * (nI + 1) + static_cast<int64_t>(split_rows) * (split_rows + 1);
     digit_syrk_kernel<ND><<<static_cast<unsigned>(tiles), kThreads, Cut<ND>::kSmemBytes, st>>>(
-        ma, mb, Rc, M, Mp, oh, ol, ld, scale_dev, exps, tri, accumulate, err);
+        ma, mb, Rc, M, Mp, oh, ol, ld, scale_dev, exps, tri, split_rows, o2h, o2l, accumulate, err);
     return check_launch();
 }
 
@@ -602,12 +631,25 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// C += C2 on row i's lower triangle (j <= i), as double-float: the split tiles' second halves
+__global__ void add_lower_kernel(const float* __restrict__ c2h, const float* __restrict__ c2l, int64_t S,
+                                 float* __restrict__ ch, float* __restrict__ cl) {
+    const int64_t i = blockIdx.y;
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j > i) return;
+    const int64_t o = i * S + j;
+    const df v = df_add({ch[o], cl[o]}, {c2h[o], c2l[o]});
+    ch[o] = v.hi;
+    cl[o] = v.lo;
+}
+
 }  // namespace tc
 
 size_t tc_lauum_workspace_bytes(int64_t S) {
     const tc::LauumPlan p = tc::lauum_plan(S);
     Sizer s;
     s.take<__nv_bfloat16>(size_t(tc::kInvDigits) * p.Sp * p.Rc);
+    s.take<float>(2 * S * S);  // the second halves of the split tiles
     s.take<unsigned>(p.Sp);
     s.take<int>(p.Sp);
     s.take<int>(1);
@@ -624,6 +666,7 @@ int tc_lauum(const float* Xh, const float* Xl, int64_t S, float* Ch, float* Cl, 
     const tc::LauumPlan p = tc::lauum_plan(S);
     Carver cv(ws, bytes);
     auto* D = cv.take<__nv_bfloat16>(size_t(tc::kInvDigits) * p.Sp * p.Rc);
+    float* C2 = cv.take<float>(2 * S * S);
     unsigned* colmax = cv.take<unsigned>(p.Sp);
     int* exps = cv.take<int>(p.Sp);
     int* err = cv.take<int>(1);
@@ -637,7 +680,18 @@ int tc_lauum(const float* Xh, const float* Xl, int64_t S, float* Ch, float* Cl, 
     tc::lauum_digits_kernel<<<dim3(static_cast<unsigned>(p.Rc / 32), static_cast<unsigned>(p.Sp / 32)), 256, 0, st>>>(
         Xh, Xl, S, p.Sp, p.Rc, colmax, exps, scale, D);
     AJ_LAUNCHED();
-    AJ_TRY(tc::launch_syrk<tc::kInvDigits>(D, p.Rc, S, p.Sp, Ch, Cl, S, scale, exps, 1, 0, err, st));
+    // row tile I sums Rc / 256 - floor(I / 2) groups; the row tiles with 3 or more are split in two, so
+    // the longest CTA sums about half the longest tile's groups (S = 1,500: 3 of 6 groups, 228 CTAs)
+    const int64_t nI = p.Sp / tc::BM, ng = p.Rc / tc::kGroupRows;
+    const int split_rows = static_cast<int>(std::min<int64_t>(nI, std::max<int64_t>(0, 2 * (ng - 3) + 2)));
+    AJ_TRY(tc::launch_syrk<tc::kInvDigits>(D, p.Rc, S, p.Sp, Ch, Cl, S, scale, exps, 1, 0, err, st, split_rows, C2,
+                                           C2 + S * S));
+    if (split_rows > 0) {
+        const int64_t rows = std::min<int64_t>(S, static_cast<int64_t>(split_rows) * tc::BM);
+        tc::add_lower_kernel<<<dim3(static_cast<unsigned>((rows + 255) / 256), static_cast<unsigned>(rows)), 256, 0,
+                               st>>>(C2, C2 + S * S, S, Ch, Cl);
+        AJ_LAUNCHED();
+    }
     tc::poison_on_error_kernel<<<1, 1, 0, st>>>(err, Ch);
     return check_launch();
 }
