@@ -59,6 +59,7 @@ enum LaneEvent {
     kEvPreDone,  // ... and is joined here
     kEvHDone,    // H's factorisation, beside A's, is done
     kEvHReady,   // H is split and its inverse buffer zeroed
+    kEvAinv,     // A^-1 is complete (its product runs beside the solve's first products)
     kEvJoin0,
     kLaneEvents = kEvJoin0 + kLaneCount
 };
@@ -119,10 +120,11 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
                           DfSpd* const* w, double* const* logdet, int* info, cudaStream_t st, float* AIh = nullptr,
                           float* AIl = nullptr, bool prepared = false);
 // x = A^-1 b refined once against A (planes), the correction through A^-1's planes when given;
-// b_split: b's planes are already in w.vec; xh/xl, when set, receive x's planes
+// b_split: b's planes are already in w.vec; xh/xl, when set, receive x's planes; ainv_ready, when
+// set, is waited for before the correction reads A^-1 (whose product may run on another stream)
 int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x,
                         cudaStream_t st, const float* AIh = nullptr, const float* AIl = nullptr, bool b_split = false,
-                        float* xh = nullptr, float* xl = nullptr);
+                        float* xh = nullptr, float* xl = nullptr, cudaEvent_t ainv_ready = nullptr);
 int df_frob_lower(const float* h, const float* l, int64_t S, double* partial, int64_t nparts, cudaStream_t st);
 
 // ---- wtilde_tc.cu (the mixed direct w_tilde on the tensor cores)

@@ -673,12 +673,24 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
         const float* fl[1] = {b.da.Ll};
         DfSpd* fw[1] = {&b.da};
         double* ld[1] = {b.logdets + 0};
-        AJ_TRY(dfspd_factor_invert_n(fh, fl, 1, 1, S, fw, ld, info, st, with_grad ? b.AIh : nullptr,
-                                     with_grad ? b.AIl : nullptr, true));
+        AJ_TRY(dfspd_factor_invert_n(fh, fl, 1, 1, S, fw, ld, info, st, nullptr, nullptr, true));
+        // with the gradient, A^-1 = L^-T L^-1 on the tensor cores on lane 4, beside the solve's first
+        // products (which need only L^-1); the solve waits for it before its correction
+        cudaEvent_t ainv_ready = nullptr;
+        if (with_grad) {
+            cudaStream_t lau = ln.s[4];
+            if (cudaEventRecord(ln.ev[kEvAinv], st) != cudaSuccess ||
+                cudaStreamWaitEvent(lau, ln.ev[kEvAinv], 0) != cudaSuccess)
+                return AJ_ERR_CUDA;
+            AJ_TRY(tc_lauum(b.da.Ih, b.da.Il, S, b.AIh, b.AIl, b.da.tcws, b.da.tcws_bytes, lau));
+            AJ_TRY(df_mirror_lower(b.AIh, b.AIl, S, lau));
+            if (cudaEventRecord(ln.ev[kEvAinv], lau) != cudaSuccess) return AJ_ERR_CUDA;
+            ainv_ready = ln.ev[kEvAinv];
+        }
         // (with the gradient, s's planes for the adjoint come out of the solve's last product)
         AJ_TRY(dfspd_solve_refined(S, b.da, b.Ah, b.Al, b.D, b.s, st, with_grad ? b.AIh : nullptr,
                                    with_grad ? b.AIl : nullptr, true, with_grad ? b.sh : nullptr,
-                                   with_grad ? b.sl : nullptr));
+                                   with_grad ? b.sl : nullptr, ainv_ready));
     }
     // H's chain (log|H|, and tr(H^-1)'s partial sums with the gradient) joins before the assembly
     if (cudaStreamWaitEvent(st, ln.ev[kEvHDone], 0) != cudaSuccess) return AJ_ERR_CUDA;

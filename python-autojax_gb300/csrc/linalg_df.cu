@@ -1370,7 +1370,8 @@ static int df_trsolve(int64_t S, DfSpd& w, const float* bh, float* uh, double* x
 // b_split: b's planes are already in w.vec (S hi floats, then S lo floats).
 // xh/xl, when set, receive the planes of the final x.
 int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, const double* b, double* x,
-                        cudaStream_t st, const float* AIh, const float* AIl, bool b_split, float* xh, float* xl) {
+                        cudaStream_t st, const float* AIh, const float* AIl, bool b_split, float* xh, float* xl,
+                        cudaEvent_t ainv_ready) {
     if (!w.Ih) return AJ_ERR_ARG;
     float* v1 = reinterpret_cast<float*>(w.vec);   // b's planes, then x0's
     float* v2 = reinterpret_cast<float*>(w.vec2);  // L^-1 b's planes, then r's
@@ -1380,6 +1381,7 @@ int dfspd_solve_refined(int64_t S, DfSpd& w, const float* Ah, const float* Al, c
     df_gemv_kernel<<<g, 256, 0, st>>>(Ah, Al, S, v1, v1 + S, b, nullptr, v2, v2 + S, 0);
     AJ_LAUNCHED();
     if (AIh) {
+        if (ainv_ready && cudaStreamWaitEvent(st, ainv_ready, 0) != cudaSuccess) return AJ_ERR_CUDA;
         df_gemv_kernel<<<g, 256, 0, st>>>(AIh, AIl, S, v2, v2 + S, nullptr, x, xh, xl, 1);
         return check_launch();
     }
