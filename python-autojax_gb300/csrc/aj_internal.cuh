@@ -148,6 +148,7 @@ struct Csc {
     float2* vdf;   // the same weights as double-float (hi, lo), converted once at build
     int* keys;     // scratch: per-chunk column histograms
     int* cursor;   // scratch: per-chunk column write offsets
+    int* part;     // scratch: per chunk-group column counts, then the groups' first offsets
 };
 enum CscMode { CSC_SUM = 0, CSC_ASSIGN = 1 };
 void csc_take(Carver& cv, int64_t M, int64_t B, int64_t S, Csc& c);

@@ -124,8 +124,23 @@ __global__ void __launch_bounds__(256)
 }
 
 // colptr[s] = sum of all counts of columns < s; off[chunk][s] = colptr[s] + counts of earlier chunks
-__global__ void csc_offsets_kernel(const int* __restrict__ hist, int64_t nchunk, int64_t S, int* __restrict__ colptr,
-                                   int* __restrict__ off) {
+// Column pointers and per-chunk write offsets from the per-chunk histograms, in three passes so the
+// long sums over chunks run spread over the GPU: per chunk-group column counts (part[g][s]), one
+// block's exclusive scan over the columns (colptr, and each group's first offset back into part),
+// then each group's chunks' offsets (off[c][s]).
+constexpr int CSC_GROUPS = 8;
+
+__global__ void csc_group_count_kernel(const int* __restrict__ hist, int64_t nchunk, int64_t S, int* __restrict__ part) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const int64_t g = blockIdx.y, per = (nchunk + CSC_GROUPS - 1) / CSC_GROUPS;
+    const int64_t c0 = g * per, c1 = min(nchunk, c0 + per);
+    int t = 0;
+    for (int64_t c = c0; c < c1; ++c) t += hist[c * S + s];
+    part[g * S + s] = t;
+}
+
+__global__ void csc_scan_kernel(int64_t S, int* __restrict__ part, int* __restrict__ colptr) {
     __shared__ int warp_tot[32];
     __shared__ int base;
     if (threadIdx.x == 0) base = 0;
@@ -133,10 +148,12 @@ __global__ void csc_offsets_kernel(const int* __restrict__ hist, int64_t nchunk,
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int64_t s0 = 0; s0 < S; s0 += blockDim.x) {
         const int64_t s = s0 + threadIdx.x;
+        int cnt[CSC_GROUPS];
         int tot = 0;
-        if (s < S) {
-#pragma unroll 8
-            for (int64_t c = 0; c < nchunk; ++c) tot += hist[c * S + s];
+#pragma unroll
+        for (int g = 0; g < CSC_GROUPS; ++g) {
+            cnt[g] = s < S ? part[g * S + s] : 0;
+            tot += cnt[g];
         }
         int x = tot;
 #pragma unroll
@@ -151,10 +168,10 @@ __global__ void csc_offsets_kernel(const int* __restrict__ hist, int64_t nchunk,
         if (s < S) {
             int run = base + before + x - tot;
             colptr[s] = run;
-#pragma unroll 8
-            for (int64_t c = 0; c < nchunk; ++c) {
-                off[c * S + s] = run;
-                run += hist[c * S + s];
+#pragma unroll
+            for (int g = 0; g < CSC_GROUPS; ++g) {
+                part[g * S + s] = run;
+                run += cnt[g];
             }
         }
         __syncthreads();
@@ -166,6 +183,19 @@ __global__ void csc_offsets_kernel(const int* __restrict__ hist, int64_t nchunk,
         __syncthreads();
     }
     if (threadIdx.x == 0) colptr[S] = base;
+}
+
+__global__ void csc_group_offsets_kernel(const int* __restrict__ hist, int64_t nchunk, int64_t S,
+                                         const int* __restrict__ part, int* __restrict__ off) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const int64_t g = blockIdx.y, per = (nchunk + CSC_GROUPS - 1) / CSC_GROUPS;
+    const int64_t c0 = g * per, c1 = min(nchunk, c0 + per);
+    int run = part[g * S + s];
+    for (int64_t c = c0; c < c1; ++c) {
+        off[c * S + s] = run;
+        run += hist[c * S + s];
+    }
 }
 
 // one warp per chunk walks its entries in order; equal columns inside a
@@ -573,6 +603,7 @@ size_t csc_bytes(int64_t M, int64_t B, int64_t S) {
     s.take<float2>(M * B);
     s.take<int>(nch * S);  // hist
     s.take<int>(nch * S);  // offsets / cursors
+    s.take<int>(CSC_GROUPS * S);  // chunk-group counts / offsets
     return s.total();
 }
 
@@ -584,6 +615,7 @@ void csc_take(Carver& cv, int64_t M, int64_t B, int64_t S, Csc& c) {
     c.vdf = cv.take<float2>(M * B);
     c.keys = cv.take<int>(nch * S);
     c.cursor = cv.take<int>(nch * S);
+    c.part = cv.take<int>(CSC_GROUPS * S);
 }
 
 int csc_build(const int64_t* idx, const double* w, const int64_t* sizes, int64_t M, int64_t B, int64_t S, CscMode mode,
@@ -595,7 +627,12 @@ int csc_build(const int64_t* idx, const double* w, const int64_t* sizes, int64_t
     if (cudaMemsetAsync(hist, 0, sizeof(int) * nch * S, st) != cudaSuccess) return AJ_ERR_CUDA;
     csc_hist_kernel<<<(unsigned)nch, 256, 0, st>>>(idx, sizes, M, B, S, mode, hist, info);
     AJ_LAUNCHED();
-    csc_offsets_kernel<<<1, 1024, 0, st>>>(hist, nch, S, c.colptr, off);
+    const dim3 gg(static_cast<unsigned>((S + 127) / 128), CSC_GROUPS);
+    csc_group_count_kernel<<<gg, 128, 0, st>>>(hist, nch, S, c.part);
+    AJ_LAUNCHED();
+    csc_scan_kernel<<<1, 1024, 0, st>>>(S, c.part, c.colptr);
+    AJ_LAUNCHED();
+    csc_group_offsets_kernel<<<gg, 128, 0, st>>>(hist, nch, S, c.part, off);
     AJ_LAUNCHED();
     csc_place_kernel<<<(unsigned)nch, 32, 0, st>>>(idx, w, sizes, M, B, S, mode, off, c.rows, c.vals, c.vdf);
     return check_launch();
