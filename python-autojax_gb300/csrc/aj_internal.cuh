@@ -114,8 +114,8 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 // S x S matrices (planes) sharing every launch; the
 // first n_inverse of them also get their inverse factor L^-1 (in w->Ih/Il),
 // computed alongside the factorisation as its panels complete.  With AIh/AIl
-// set (planes, S x S), the first matrix's inverse A^-1 = L^-T L^-1 is built
-// up the same way, one finished block row of L^-1 at a time.
+// set (planes, S x S; the first matrix's DfSpd carved with_ainv), the first
+// matrix's inverse A^-1 = L^-T L^-1 follows on the tensor cores (tc_lauum).
 int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int count, int n_inverse, int64_t S,
                           DfSpd* const* w, double* const* logdet, int* info, cudaStream_t st, float* AIh = nullptr,
                           float* AIl = nullptr, bool prepared = false);

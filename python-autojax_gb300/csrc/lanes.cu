@@ -3,8 +3,9 @@
 // The blocked factorisations are chains of small, latency-bound launches.  They
 // run faster as concurrent chains: the critical one (the pivot panels) on the
 // highest-priority stream, and at one lower priority the bulk of each trailing
-// update, the triangular inverses, which need only finished panels (one lane
-// per matrix), and A^-1 = L^-T L^-1, which needs only finished rows of L^-1.
+// update and the triangular inverses, which need only finished panels (one lane
+// per matrix); the float64 path's A^-1 = L^-T L^-1 also streams on a lane, as
+// rows of L^-1 finish.
 // (Ranking the bulk lane below or above the others measured 23 us and 5 us
 // slower per evaluation at K = 1e6.)  Every fork starts
 // with an event recorded on the caller's stream and every join ends with the

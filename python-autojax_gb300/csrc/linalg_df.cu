@@ -2,10 +2,11 @@
 //
 // GB300 issues ~62x more float32 than float64 operations per clock, so the
 // S^3 work of the evaluation (two Cholesky factorisations, two triangular
-// inverses, A^-1 = L^-T L^-1) runs as double-float on the float32 pipe:
-// ~15 float32 operations per multiply-add with ~2^-47 relative rounding
-// (float64 keeps 2^-53; the inversion's conditioning needs better than
-// float32's 2^-24, see the mixed-precision notes in the design document).
+// inverses) runs as double-float on the float32 pipe: ~11-15 float32
+// operations per multiply-add with ~2^-47 relative rounding (float64 keeps
+// 2^-53; the inversion's conditioning needs better than float32's 2^-24, see
+// the mixed-precision notes in the design document).  A^-1 = L^-T L^-1 runs on
+// the tensor cores as exact digit products (wtilde_tc.cu).
 //
 // Matrices are row-major S x S with separate hi and lo float planes.
 // Blocked algorithms use NB = 32; the diagonal block of every step is
