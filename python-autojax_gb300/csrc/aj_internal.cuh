@@ -116,9 +116,12 @@ int gemm_df(bool ta, bool tb, int64_t m, int64_t n, int64_t k, bool neg, const f
 // computed alongside the factorisation as its panels complete.  With AIh/AIl
 // set (planes, S x S; the first matrix's DfSpd carved with_ainv), the first
 // matrix's inverse A^-1 = L^-T L^-1 follows on the tensor cores (tc_lauum).
+// f32_inverse: L^-1 in plain float32 from L's hi plane (into Ih; Il keeps what it held), for a
+// matrix whose L^-1 serves only a trace that enters the result scaled down (the regularisation
+// matrix's tr(H^-1))
 int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int count, int n_inverse, int64_t S,
                           DfSpd* const* w, double* const* logdet, int* info, cudaStream_t st, float* AIh = nullptr,
-                          float* AIl = nullptr, bool prepared = false);
+                          float* AIl = nullptr, bool prepared = false, bool f32_inverse = false);
 // x = A^-1 b refined once against A (planes), the correction through A^-1's planes when given;
 // b_split: b's planes are already in w.vec; xh/xl, when set, receive x's planes; ainv_ready, when
 // set, is waited for before the correction reads A^-1 (whose product may run on another stream)

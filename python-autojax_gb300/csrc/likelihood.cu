@@ -612,7 +612,10 @@ int aj_log_evidence(const aj_problem* p, int precision, int with_grad, double* o
             const float* hl[1] = {b.dh.Ll};
             DfSpd* hw[1] = {&b.dh};
             double* hld[1] = {b.logdets + 1};
-            rc = dfspd_factor_invert_n(hh, hl, 1, with_grad ? 1 : 0, S, hw, hld, info, hlane, nullptr, nullptr, true);
+            // (L^-1 of H in float32: tr(H^-1) enters dlogE/dlambda as 1e-8 tr(H^-1) / lambda against
+            // S / lambda, and the deflated H is well conditioned, so float32 moves it by ~1e-12)
+            rc = dfspd_factor_invert_n(hh, hl, 1, with_grad ? 1 : 0, S, hw, hld, info, hlane, nullptr, nullptr, true,
+                                       true);
             // tr(H^-1)'s partial sums for dlogE/dlambda here too, long before the evaluation's tail
             if (rc == AJ_OK && with_grad) rc = df_frob_lower(b.dh.Ih, b.dh.Il, S, b.fpart, b.nfrob, hlane);
             if (cudaEventRecord(ln.ev[kEvHDone], hlane) != cudaSuccess) return AJ_ERR_CUDA;

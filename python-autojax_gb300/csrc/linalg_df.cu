@@ -943,6 +943,120 @@ __global__ void __launch_bounds__(256)
         }
 }
 
+// ------------------------------------------------- L^-1 in float32
+//
+// The same two L^-1 steps in plain float32, from L's hi plane, into X's hi plane (its lo plane is
+// left as it is).  For a matrix whose L^-1 serves only a trace that enters its result scaled down:
+// the regularisation matrix's tr(H^-1) enters dlogE/dlambda as 1e-8 tr(H^-1) / lambda against
+// S / lambda, and H is deflated (condition ~1e3), so float32's ~1e-6 on the trace moves dlogE/dlambda
+// by ~1e-12 relative at the K=1e6 configuration, for 1 float32 instruction a multiply-add instead of
+// 11.
+
+__global__ void __launch_bounds__(256)
+    f32_trtri_step_kernel(DfMats mats, int64_t S, int64_t kb) {
+    const float* __restrict__ Lh = pick(mats.Lh, blockIdx.y);
+    float* __restrict__ Ih = pick(mats.Ih, blockIdx.y);
+    const float* __restrict__ dh = pick(mats.dh, blockIdx.y);
+    __shared__ float as[32][33], bs[32][33];  // as[r][k] = L[i0 + r][p0 + k], bs[k][c] = X[p0 + k][j0 + c]
+    const int64_t nbt = (S + DNB - 1) / DNB;
+    const int64_t ncol = kb + 1;
+    const int64_t ti = kb + 1 + blockIdx.x / ncol, tj = blockIdx.x % ncol;
+    if (ti >= nbt) return;
+    const int tid = threadIdx.x;
+    const int64_t i0 = ti * DNB, j0 = tj * DNB, p0 = kb * DNB;
+    const int r = tid >> 3, q = tid & 7;
+    float acc[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        const int64_t gi = i0 + r, gj = j0 + q + 8 * t;
+        acc[t] = gi < S && gj < S ? Ih[gi * S + gj] : 0.f;
+    }
+    for (int e = tid; e < DNB * DNB; e += 256) {
+        const int rr = e / DNB, c = e % DNB;
+        as[rr][c] = i0 + rr < S && p0 + c < S ? Lh[(i0 + rr) * S + p0 + c] : 0.f;
+        bs[rr][c] = p0 + rr < S && j0 + c < S ? Ih[(p0 + rr) * S + j0 + c] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < DNB; ++k) {
+        const float x = as[r][k];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) acc[t] = fmaf(x, bs[k][q + 8 * t], acc[t]);
+    }
+    if (ti != kb + 1) {
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int64_t gi = i0 + r, gj = j0 + q + 8 * t;
+            if (gi < S && gj < S) Ih[gi * S + gj] = acc[t];
+        }
+        return;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < 4; ++t) as[r][q + 8 * t] = acc[t];
+    for (int e = tid; e < DNB * DNB; e += 256) bs[e / DNB][e % DNB] = dh[(kb + 1) * DNB * DNB + e];
+    __syncthreads();
+    float out[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int p = 0; p < DNB; ++p) {
+        const float d = bs[r][p];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) out[t] = fmaf(d, as[p][q + 8 * t], out[t]);
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        const int64_t gi = i0 + r, gj = j0 + q + 8 * t;
+        if (gi < S && gj < S) Ih[gi * S + gj] = -out[t];
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    f32_trtri64_kernel(DfMats mats, int64_t S, int64_t kb) {
+    const float* __restrict__ Lh = pick(mats.Lh, blockIdx.y);
+    float* __restrict__ Ih = pick(mats.Ih, blockIdx.y);
+    __shared__ float a[DNB][T64 + 1], b[DNB][T64 + 1];  // a[k][row], b[k][column]
+    const int64_t ncol = (kb + 1) * DNB;
+    const int64_t nJ = (ncol + T64 - 1) / T64;
+    const int64_t I = blockIdx.x / nJ, J = blockIdx.x % nJ;
+    const int64_t i0 = (kb + 2) * DNB + I * T64, j0 = J * T64, p0 = kb * DNB;
+    if (i0 >= S) return;
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t gi = i0 + ty + 16 * i, gj = j0 + tx + 16 * j;
+            acc[i][j] = gi < S && gj < ncol ? Ih[gi * S + gj] : 0.f;
+        }
+    for (int e = tid; e < T64 * DNB; e += 256) {
+        const int rr = e / DNB, k = e % DNB;  // a: rows of L's block column kb
+        a[k][rr] = i0 + rr < S && p0 + k < S ? Lh[(i0 + rr) * S + p0 + k] : 0.f;
+        const int k2 = e / T64, c = e % T64;  // b: block row kb of X
+        b[k2][c] = p0 + k2 < S && j0 + c < S ? Ih[(p0 + k2) * S + j0 + c] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int k = 0; k < DNB; ++k) {
+        float av[4], bv[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) av[i] = a[k][ty + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) bv[j] = b[k][tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t gi = i0 + ty + 16 * i, gj = j0 + tx + 16 * j;
+            if (gi < S && gj < ncol) Ih[gi * S + gj] = acc[i][j];
+        }
+}
+
 __global__ void df_mirror_lower_kernel(float* __restrict__ h, float* __restrict__ l, int64_t S) {
     for (int64_t i = blockIdx.y; i < S; i += gridDim.y)
         for (int64_t j = i + 1 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < S;
@@ -1219,7 +1333,7 @@ static int g_tile64_min[2] = {128, 128};  // trailing update, L^-1 step
 // is done, so it trails the factorisation by one panel.
 int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int count, int n_inverse, int64_t S,
                           DfSpd* const* w, double* const* logdet, int* info, cudaStream_t st, float* AIh,
-                          float* AIl, bool prepared) {
+                          float* AIl, bool prepared, bool f32_inverse) {
     if (S <= 0) return AJ_OK;
     if (count < 1 || count > 2 || n_inverse < 0 || n_inverse > count) return AJ_ERR_ARG;
     if ((AIh || AIl) && (!AIh || !AIl || n_inverse < 1)) return AJ_ERR_ARG;
@@ -1317,10 +1431,16 @@ int dfspd_factor_invert_n(const float* const* Ah, const float* const* Al, int co
             const int64_t tiles = (big ? 1 : nbt - kb - 1) * (kb + 1);
             for (int z = 0; z < n_inverse; ++z) {
                 AJ_TRY(lane_wait(ln, 2 + z, kEvDiag));
-                df_trtri_step_kernel<<<(unsigned)tiles, 256, 0, ln.s[2 + z]>>>(one[z], S, kb);
+                if (f32_inverse)
+                    f32_trtri_step_kernel<<<(unsigned)tiles, 256, 0, ln.s[2 + z]>>>(one[z], S, kb);
+                else
+                    df_trtri_step_kernel<<<(unsigned)tiles, 256, 0, ln.s[2 + z]>>>(one[z], S, kb);
                 AJ_LAUNCHED();
                 if (big) {
-                    df_trtri64_kernel<<<(unsigned)(nI * nJ), 256, 0, ln.s[2 + z]>>>(one[z], S, kb);
+                    if (f32_inverse)
+                        f32_trtri64_kernel<<<(unsigned)(nI * nJ), 256, 0, ln.s[2 + z]>>>(one[z], S, kb);
+                    else
+                        df_trtri64_kernel<<<(unsigned)(nI * nJ), 256, 0, ln.s[2 + z]>>>(one[z], S, kb);
                     AJ_LAUNCHED();
                 }
             }
