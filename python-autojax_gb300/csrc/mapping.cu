@@ -384,22 +384,63 @@ __global__ void __launch_bounds__(128, 8)
 // With the grid pixel-fastest, (threads in flight x 4 columns x 4 pixels) / S columns of X are
 // live, about 63 MB at M = 9,504, S = 1,500, inside L2; 8 pixels a block (32-byte stores) kept
 // twice that and read X 1.95 times from DRAM, 60 us slower per evaluation.
+//
+// The rows are latency-bound loads (long-scoreboard stalls, 24% warps active with a group of
+// four entries double-buffered in registers).  Each thread instead streams its own 16-byte pieces
+// of the next kTrDepth groups into a private ring in shared memory with cp.async (no registers
+// held while they fly, no barrier: a thread reads only what it copied), so kTrDepth x 128 bytes a
+// thread are in flight.
 constexpr int kTrPix = 4;
 constexpr int kTrCols = 512;
+constexpr int kTrThreads = kTrCols / 4;
+constexpr int kTrDepth = 2;  // groups of four entries in flight a thread
 
-__global__ void __launch_bounds__(128)
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// ring[((slot * 4 + u) * 2 + plane) * kTrThreads + thread]: a warp's pieces of one entry and
+// plane are 512 contiguous bytes
+template <int D>
+constexpr size_t tr_ring_bytes() {
+    return sizeof(float4) * D * 4 * 2 * kTrThreads;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kTrThreads)
     csc_spmm_t_df_tr_kernel(const int* __restrict__ colptr, const int* __restrict__ rows,
                             const float2* __restrict__ vdf, const float* __restrict__ Xh,
                             const float* __restrict__ Xl, int64_t ld_x, int64_t cols, int64_t S,
                             float* __restrict__ Oh, float* __restrict__ Ol, int64_t ld_out) {
+    extern __shared__ float4 ring[];
     __shared__ int srow[kGatherStage];
     __shared__ float2 sw[kGatherStage];
     __shared__ float th[kTrPix][kTrCols], tl[kTrPix][kTrCols];
     const int64_t s0 = (int64_t)blockIdx.x * kTrPix;
     const int64_t cbase = (int64_t)blockIdx.y * kTrCols;
-    const int cl = threadIdx.x * 4;
+    const int tid = threadIdx.x;
+    const int cl = tid * 4;
     const int64_t c0 = cbase + cl;
     const bool live = c0 < cols;
+    // copies group q's four entries (a group past the column's end repeats the segment's first
+    // row, which then meets weight 0) into ring slot q % D
+    auto issue = [&](int q, int n) {
+        float4* base = ring + (q % D) * 4 * 2 * kTrThreads + tid;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int qq = q * 4 + u < n ? q * 4 + u : 0;
+            const int64_t off = (int64_t)srow[qq] * ld_x + c0;
+            cp_async16(base + (u * 2 + 0) * kTrThreads, Xh + off);
+            cp_async16(base + (u * 2 + 1) * kTrThreads, Xl + off);
+        }
+    };
     for (int sp = 0; sp < kTrPix; ++sp) {
         const int64_t s = s0 + sp;
         if (s >= S) break;
@@ -409,39 +450,38 @@ __global__ void __launch_bounds__(128)
         for (int seg = b; seg < e; seg += kGatherStage) {
             const int n = min(kGatherStage, e - seg);
             __syncthreads();  // the previous pass's reads of the staged entries are done
-            for (int t = threadIdx.x; t < n; t += blockDim.x) {
+            for (int t = tid; t < n; t += blockDim.x) {
                 srow[t] = rows[seg + t];
                 sw[t] = vdf[seg + t];
             }
             __syncthreads();
             if (!live) continue;
-            float4 h[4], l[4];
-            float2 a[4];
-            gather_group(srow, sw, Xh, Xl, ld_x, c0, 0, n, h, l, a);
-            for (int q = 0; q < n; q += 4) {
-                float4 hn[4], ln[4];
-                float2 an[4];
-                const bool more = q + 4 < n;
-                if (more) gather_group(srow, sw, Xh, Xl, ld_x, c0, q + 4, n, hn, ln, an);
+            const int ng = (n + 3) / 4;
+#pragma unroll
+            for (int q = 0; q < D; ++q) {
+                if (q < ng) issue(q, n);
+                cp_async_commit();  // one group a step, empty or not, so the wait counts stay fixed
+            }
+            for (int q = 0; q < ng; ++q) {
+                cp_async_wait<D - 1>();  // this thread's copies of group q have landed
+                const float4* base = ring + (q % D) * 4 * 2 * kTrThreads + tid;
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
-                    const df w = {a[u].x, a[u].y};
-                    df_fma_lazy(acc[0], w, {h[u].x, l[u].x});
-                    df_fma_lazy(acc[1], w, {h[u].y, l[u].y});
-                    df_fma_lazy(acc[2], w, {h[u].z, l[u].z});
-                    df_fma_lazy(acc[3], w, {h[u].w, l[u].w});
+                    const float4 h = base[(u * 2 + 0) * kTrThreads];
+                    const float4 l = base[(u * 2 + 1) * kTrThreads];
+                    const float2 a2 = q * 4 + u < n ? sw[q * 4 + u] : make_float2(0.f, 0.f);
+                    const df w = {a2.x, a2.y};
+                    df_fma_lazy(acc[0], w, {h.x, l.x});
+                    df_fma_lazy(acc[1], w, {h.y, l.y});
+                    df_fma_lazy(acc[2], w, {h.z, l.z});
+                    df_fma_lazy(acc[3], w, {h.w, l.w});
                 }
                 if (++group % 2 == 0)
 #pragma unroll
                     for (int v = 0; v < 4; ++v) df_renorm(acc[v]);
-                if (more) {
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        h[u] = hn[u];
-                        l[u] = ln[u];
-                        a[u] = an[u];
-                    }
-                }
+                // the slot's values are in registers and consumed: refill it
+                if (q + D < ng) issue(q + D, n);
+                cp_async_commit();
             }
         }
         if (live) {
@@ -453,10 +493,11 @@ __global__ void __launch_bounds__(128)
             }
         }
     }
+    cp_async_wait<0>();
     __syncthreads();
     const int np = (int)(S - s0 < kTrPix ? S - s0 : kTrPix);
     const bool vec = np == kTrPix && ld_out % 4 == 0 && s0 % 4 == 0;
-    for (int r = threadIdx.x; r < kTrCols; r += blockDim.x) {
+    for (int r = tid; r < kTrCols; r += blockDim.x) {
         const int64_t c = cbase + r;
         if (c >= cols) break;
         float* oh = Oh + c * ld_out + s0;
@@ -689,9 +730,18 @@ int csc_spmm_t_df_tr(const Csc& c, int64_t S, const float* Xh, const float* Xl, 
                      (reinterpret_cast<uintptr_t>(Xl) % 16 == 0) && (reinterpret_cast<uintptr_t>(Oh) % 16 == 0) &&
                      (reinterpret_cast<uintptr_t>(Ol) % 16 == 0);
     if (!vec) return AJ_ERR_ARG;
+    static bool attr[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return AJ_ERR_CUDA;
+    if (dev < 64 && !attr[dev]) {
+        if (cudaFuncSetAttribute(csc_spmm_t_df_tr_kernel<kTrDepth>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tr_ring_bytes<kTrDepth>()) != cudaSuccess)
+            return AJ_ERR_CUDA;
+        attr[dev] = true;
+    }
     dim3 grid((unsigned)((S + kTrPix - 1) / kTrPix), (unsigned)((cols + kTrCols - 1) / kTrCols));
-    csc_spmm_t_df_tr_kernel<<<grid, kTrCols / 4, 0, st>>>(c.colptr, c.rows, c.vdf, Xh, Xl, ld_x, cols, S, Oh, Ol,
-                                                           ld_out);
+    csc_spmm_t_df_tr_kernel<kTrDepth><<<grid, kTrThreads, tr_ring_bytes<kTrDepth>(), st>>>(
+        c.colptr, c.rows, c.vdf, Xh, Xl, ld_x, cols, S, Oh, Ol, ld_out);
     return check_launch();
 }
 
