@@ -165,8 +165,9 @@ __device__ __forceinline__ void store_row(float* __restrict__ oh, float* __restr
 // i cut at its own power of two).  With tri, a digit row k is zero for k < i (the panel is an upper
 // triangle, as the transpose of L^-1 is): a tile starts at the group holding its first row.  The
 // tiles of the first split_rows row tiles (the ones with the most groups then) are split in two:
-// their CTA sums the first half of the groups into out, and one of the nI (nI + 1)-plus CTAs the
-// second half into out2 (the caller adds out2 to out).
+// their CTA sums the first half of the groups into out, and one of split_rows (split_rows + 1)
+// extra CTAs, launched ahead of the nI (nI + 1) tiles, the second half into out2 (the caller adds
+// out2 to out).
 template <int ND>
 __global__ void __launch_bounds__(kThreads, 1)
     digit_syrk_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
@@ -179,12 +180,16 @@ __global__ void __launch_bounds__(kThreads, 1)
     Shared* sh = reinterpret_cast<Shared*>(base + size_t(kStages) * Cut<ND>::kStageBytes);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int64_t I, J;
-    const int64_t nI = Mp / BM, ntiles = nI * (nI + 1);
+    const int64_t nI = Mp / BM;
+    // The split tiles' second halves come first: with one CTA an SM the grid runs in about one and
+    // a half waves, and the second halves are among the longest CTAs (the first row tiles sum the
+    // most groups), so they start in the first wave and the short tiles fill in behind them.
+    const int64_t nsecond = static_cast<int64_t>(split_rows) * (split_rows + 1);
     int part = 0;  // 1: the second half of a split tile
-    if (blockIdx.x < ntiles) {
-        tile_of(blockIdx.x, nI, I, J);
+    if (blockIdx.x >= nsecond) {
+        tile_of(blockIdx.x - nsecond, nI, I, J);
     } else {
-        int64_t e = blockIdx.x - ntiles;  // split tiles in row-major order: 2I + 2 in row tile I
+        int64_t e = blockIdx.x;  // split tiles in row-major order: 2I + 2 in row tile I
         I = 0;
         while (e >= 2 * I + 2) {
             e -= 2 * I + 2;
