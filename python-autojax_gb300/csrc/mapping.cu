@@ -378,19 +378,20 @@ __global__ void __launch_bounds__(128, 8)
 }
 
 // The same gather with the output transposed (out[c][s], e.g. Omega = (T^T W)^T): a block takes
-// 4 source pixels over one 512-column chunk, one pixel after another with the entry order, the
+// 2 source pixels over one 512-column chunk, one pixel after another with the entry order, the
 // grouping and the renormalisation of csc_spmm_t_df_vec_kernel (so each sum is bit-identical),
-// keeps the results in shared memory and stores 4 consecutive pixels (16 bytes) per output row.
-// With the grid pixel-fastest, (threads in flight x 4 columns x 4 pixels) / S columns of X are
-// live, about 63 MB at M = 9,504, S = 1,500, inside L2; 8 pixels a block (32-byte stores) kept
-// twice that and read X 1.95 times from DRAM, 60 us slower per evaluation.
+// keeps the results in shared memory and stores 2 consecutive pixels (8 bytes) per output row.
+// With the grid pixel-fastest, (threads in flight x 4 columns x 2 pixels) / S columns of X are
+// live at once, inside L2; 8 pixels a block (32-byte stores) kept 126 MB live at M = 9,504,
+// S = 1,500 and read X 1.95 times from DRAM, 60 us slower per evaluation.
 //
 // The rows are latency-bound loads (long-scoreboard stalls, 24% warps active with a group of
 // four entries double-buffered in registers).  Each thread instead streams its own 16-byte pieces
 // of the next kTrDepth groups into a private ring in shared memory with cp.async (no registers
 // held while they fly, no barrier: a thread reads only what it copied), so kTrDepth x 128 bytes a
-// thread are in flight.
-constexpr int kTrPix = 4;
+// thread are in flight.  With the ring, 2 pixels a block (5 blocks an SM by shared memory)
+// measured faster than 4 (4 blocks an SM).
+constexpr int kTrPix = 2;
 constexpr int kTrCols = 512;
 constexpr int kTrThreads = kTrCols / 4;
 constexpr int kTrDepth = 2;  // groups of four entries in flight a thread
@@ -496,15 +497,15 @@ __global__ void __launch_bounds__(kTrThreads)
     cp_async_wait<0>();
     __syncthreads();
     const int np = (int)(S - s0 < kTrPix ? S - s0 : kTrPix);
-    const bool vec = np == kTrPix && ld_out % 4 == 0 && s0 % 4 == 0;
+    const bool vec = np == kTrPix && ld_out % 2 == 0 && s0 % 2 == 0;
     for (int r = tid; r < kTrCols; r += blockDim.x) {
         const int64_t c = cbase + r;
         if (c >= cols) break;
         float* oh = Oh + c * ld_out + s0;
         float* ol = Ol + c * ld_out + s0;
         if (vec) {
-            reinterpret_cast<float4*>(oh)[0] = make_float4(th[0][r], th[1][r], th[2][r], th[3][r]);
-            reinterpret_cast<float4*>(ol)[0] = make_float4(tl[0][r], tl[1][r], tl[2][r], tl[3][r]);
+            reinterpret_cast<float2*>(oh)[0] = make_float2(th[0][r], th[1][r]);
+            reinterpret_cast<float2*>(ol)[0] = make_float2(tl[0][r], tl[1][r]);
         } else {
             for (int sp = 0; sp < np; ++sp) {
                 oh[sp] = th[sp][r];
