@@ -281,8 +281,11 @@ class LogEvidence:
         self._h_idx[...] = pix_indexes
         self._h_w[...] = pix_weights
         nb = np.asarray(neighbors)
-        self._h_nb[...] = -1
-        self._h_nb[:, : nb.shape[1]] = nb
+        if nb.shape[1] == self._h_nb.shape[1]:
+            self._h_nb[...] = nb
+        else:
+            self._h_nb[...] = -1
+            self._h_nb[:, : nb.shape[1]] = nb
         self._h_nsz[...] = neighbors_sizes
         self._h_coef[0] = coefficient
         self._in.copy_(self._h_in, non_blocking=True)
