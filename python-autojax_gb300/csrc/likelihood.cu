@@ -207,7 +207,8 @@ __device__ __forceinline__ bool wg_entry(const int64_t* row, int64_t B, int64_t 
 // Omega_m . s and up to kWgDots products Omega_m . A^-1_sp side by side (16-byte
 // loads when every row is 16-byte aligned), so a thread's dependent chain is
 // S / kWgThreads steps long; a block reduction in fixed order finishes them.
-constexpr int kWgThreads = 128;
+// (64 threads measured faster than 32, 96, 128, 256 or 384 across the batch and one evaluation)
+constexpr int kWgThreads = 64;
 constexpr int kWgDots = 4;
 
 __global__ void __launch_bounds__(kWgThreads)
