@@ -48,13 +48,13 @@ class Config:
 
 
 CONFIGS = {
-    # BASELINE configs[0]: K=2e3, 30x30 at 0.1", r=1.2", 16x16 rectangular bilinear source, lam=1
+    # the small CPU-runnable inversion: K=2e3, 30x30 at 0.1", r=1.2", 16x16 rectangular bilinear source, lam=1
     "cfg1": Config("cfg1", 2_000, 30, 0.1, 1.2, 256, "rect", 0.8, 1.5, 1.0, 101),
-    # configs[1]: K=1e5, 80x80 at 0.05", r=2", S=1000 Delaunay
+    # the mid-size float64 inversion: K=1e5, 80x80 at 0.05", r=2", S=1000 Delaunay
     "cfg2": Config("cfg2", 100_000, 80, 0.05, 2.0, 1_000, "delaunay", 0.8, 1.5, 0.3, 202),
-    # configs[2]: K=1e6, 100x100 at 0.04", r=2.4", S=1500 Delaunay
+    # the large-K mixed-precision inversion: K=1e6, 100x100 at 0.04", r=2.4", S=1500 Delaunay
     "cfg3": Config("cfg3", 1_000_000, 100, 0.04, 2.4, 1_500, "delaunay", 0.8, 1.5, 1.0, 303),
-    # configs[4]: K=5e5, ~8000 image pixels (100x100 at 0.04", r=2.0"), S in [500, 2000]
+    # the batched evaluations: K=5e5, ~8000 image pixels (100x100 at 0.04", r=2.0"), S in [500, 2000]
     "cfg5": Config("cfg5", 500_000, 100, 0.04, 2.0, 1_000, "delaunay", 0.8, 1.5, 1.0, 505),
 }
 
