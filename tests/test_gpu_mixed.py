@@ -263,6 +263,25 @@ def test_mixed_matches_fp64_at_multi_chunk_sizes(aj, config, K):
         assert abs(out["mixed"][0] - out["fp64"][0]) <= 1e-7 * abs(out["fp64"][0]), (lam, out)
 
 
+@pytest.mark.parametrize("M,S", [(1028, 997), (1032, 7), (1030, 257)])
+def test_mixed_curvature_gather_edges(aj, M, S):
+    """The mixed F through the double-float gathers against the float64 products, on inputs that
+    reach their edge cases: an odd source-pixel count (the transposed gather's last block holds a
+    single pixel), source pixels with more entries than one staging pass (several passes and a
+    padded last group of four), rows ended early by -1 and repeated indices, and M not a multiple
+    of 4 (the untransposed gather, then a transpose)."""
+    rng = np.random.default_rng(M + S)
+    W = rng.standard_normal((M, M))
+    W = (W + W.T) / 2
+    idx = rng.integers(0, S, size=(M, 3))
+    idx[:300, 0] = 0  # source pixel 0 gets at least 300 entries
+    idx[::7, 2] = -1
+    w = rng.random((M, 3))
+    F = aj.curvature_matrix_via_w_wilde_sparse_mapping_matrix_from(W, idx, w, S, precision="mixed")
+    F64 = aj.curvature_matrix_via_w_wilde_sparse_mapping_matrix_from(W, idx, w, S)
+    np.testing.assert_allclose(F, F64, rtol=0, atol=1e-12 * np.abs(F64).max())
+
+
 def test_mixed_weight_gradient_ragged_rows(aj):
     """S = 101 (Omega's and A^-1's rows are not 16-byte aligned, so the gradient takes its scalar
     loads) and mapping rows padded to B = 7: later repeats that overwrite earlier entries, entries
