@@ -1145,7 +1145,10 @@ __global__ void df_trmv_t_sum_kernel(const float* __restrict__ ph, const float* 
 
 // y = A x, y = b - A x when b is set, or y += A x with add, for a full
 // double-float A (x as planes; b, y float64, y also as planes when yh is set);
-// one warp per row, four independent accumulators per lane
+// one warp per row, four independent accumulators per lane.  With 16-byte rows
+// the loads are float4, three a lane and operand in flight (the refined solve's
+// last product sits on the evaluation's tail: 2.168 against 2.212 ms an
+// evaluation in one A/B pair)
 __global__ void __launch_bounds__(256)
     df_gemv_kernel(const float* __restrict__ Ah, const float* __restrict__ Al, int64_t S,
                    const float* __restrict__ xh, const float* __restrict__ xl, const double* __restrict__ b,
@@ -1156,11 +1159,48 @@ __global__ void __launch_bounds__(256)
     df acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     const float* rh = Ah + i * S;
     const float* rl = Al + i * S;
-    int64_t j = lane;
-    for (; j + 96 < S; j += 128)
+    const uintptr_t bits = reinterpret_cast<uintptr_t>(rh) | reinterpret_cast<uintptr_t>(rl) |
+                           reinterpret_cast<uintptr_t>(xh) | reinterpret_cast<uintptr_t>(xl);
+    if ((S & 3) == 0 && (bits & 15) == 0) {
+        // 16-byte loads, three a lane and operand in flight; accumulator u takes component u
+        const float4* h4 = reinterpret_cast<const float4*>(rh);
+        const float4* l4 = reinterpret_cast<const float4*>(rl);
+        const float4* xh4 = reinterpret_cast<const float4*>(xh);
+        const float4* xl4 = reinterpret_cast<const float4*>(xl);
+        const int64_t n4 = S / 4;
+        int64_t q = lane;
+        for (; q + 64 < n4; q += 96) {
+            float4 a[3], b[3], c[3], d[3];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) df_fma_acc(acc[u], {rh[j + 32 * u], rl[j + 32 * u]}, {xh[j + 32 * u], xl[j + 32 * u]});
-    for (; j < S; j += 32) df_fma_acc(acc[0], {rh[j], rl[j]}, {xh[j], xl[j]});
+            for (int u = 0; u < 3; ++u) {
+                a[u] = h4[q + 32 * u];
+                b[u] = l4[q + 32 * u];
+                c[u] = xh4[q + 32 * u];
+                d[u] = xl4[q + 32 * u];
+            }
+#pragma unroll
+            for (int u = 0; u < 3; ++u) {
+                df_fma_acc(acc[0], {a[u].x, b[u].x}, {c[u].x, d[u].x});
+                df_fma_acc(acc[1], {a[u].y, b[u].y}, {c[u].y, d[u].y});
+                df_fma_acc(acc[2], {a[u].z, b[u].z}, {c[u].z, d[u].z});
+                df_fma_acc(acc[3], {a[u].w, b[u].w}, {c[u].w, d[u].w});
+            }
+        }
+        for (; q < n4; q += 32) {
+            const float4 a = h4[q], b = l4[q], c = xh4[q], d = xl4[q];
+            df_fma_acc(acc[0], {a.x, b.x}, {c.x, d.x});
+            df_fma_acc(acc[1], {a.y, b.y}, {c.y, d.y});
+            df_fma_acc(acc[2], {a.z, b.z}, {c.z, d.z});
+            df_fma_acc(acc[3], {a.w, b.w}, {c.w, d.w});
+        }
+    } else {
+        int64_t j = lane;
+        for (; j + 96 < S; j += 128)
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                df_fma_acc(acc[u], {rh[j + 32 * u], rl[j + 32 * u]}, {xh[j + 32 * u], xl[j + 32 * u]});
+        for (; j < S; j += 32) df_fma_acc(acc[0], {rh[j], rl[j]}, {xh[j], xl[j]});
+    }
     const double v = warp_sum(df_to(df_add(df_add(acc[0], acc[1]), df_add(acc[2], acc[3]))));
     if (lane == 0) store_y(b ? b[i] - v : v, i, y, yh, yl, add != 0);
 }
