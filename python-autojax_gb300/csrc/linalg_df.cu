@@ -1147,8 +1147,7 @@ __global__ void df_trmv_t_sum_kernel(const float* __restrict__ ph, const float* 
 // double-float A (x as planes; b, y float64, y also as planes when yh is set);
 // one warp per row, four independent accumulators per lane.  With 16-byte rows
 // the loads are float4, three a lane and operand in flight (the refined solve's
-// last product sits on the evaluation's tail: 2.168 against 2.212 ms an
-// evaluation in one A/B pair)
+// last product sits on the evaluation's tail)
 __global__ void __launch_bounds__(256)
     df_gemv_kernel(const float* __restrict__ Ah, const float* __restrict__ Al, int64_t S,
                    const float* __restrict__ xh, const float* __restrict__ xl, const double* __restrict__ b,
